@@ -1,0 +1,440 @@
+"""Benchmark of the SkelCL skeleton path on one GB300.
+
+Headline workload (one "step"): inclusive Scan(int32 add) over N = 2^28 values
+uniform in {0..1000} (seed 0), then Map(x -> x mod 7919) in place -- the
+integer scan + map configuration.  The inclusive scan is the library's
+SCL_SHAPE_INCLUSIVE form of the reference's exclusive Scan (= exclusive (+) x).
+
+  value      algorithmic HBM bytes / s over the timed steps, inputs resident
+             in HBM (scan 2*4N + map 2*4N bytes per step)
+  e2e        the same metric through the C ABI with pinned HOST buffers: every
+             step copies the input in and the result out
+  roofline   the dominant kernel (the scan) against the measured HBM copy
+             bandwidth (MEASURED_PEAKS.json)
+  skeletons  secondary per-skeleton figures (dot product, float scan and its
+             adjoint, MapOverlap 8192^2 R=5, AllPairs 8192x4096x8192,
+             Manhattan AllPairs), each against its own roofline
+
+--impl reference times the CPU restatement of the same workload (the
+reference SkelCL needs an OpenCL platform and libclang, neither of which
+exists on this pool) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_SCAN = 1 << 28
+MOD = 7919
+BYTES_SCAN = 2 * 4 * N_SCAN
+BYTES_MAP = 2 * 4 * N_SCAN
+METRIC = "HBM GB/s (int32 inclusive Scan + Map(x mod 7919), N=2^28)"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), float(d.get("bf16_tflops", 1876.6)), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def traffic_table():
+    """Per-launch DRAM bytes from the committed ncu summaries (kernel -> bytes)."""
+    t = {}
+    p = ROOT / "profiles" / "traffic_per_launch.txt"
+    if p.exists():
+        for line in p.read_text().splitlines():
+            line = line.split("#", 1)[0].strip()
+            if line:
+                k, v = line.split()[:2]
+                t[k] = float(v)
+    return t
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def timed(S, fn, steps: int, warmup: int, kernel_events=None):
+    """Warm-up, then time exactly `steps` calls of fn with events on the
+    library stream (synchronised on both sides)."""
+    for _ in range(warmup):
+        fn()
+    S.sync()
+    e0, e1 = S.Event(), S.Event()
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    S.sync()
+    return e0.elapsed_ms(e1) / steps
+
+
+def run_gpu(args):
+    import oracle
+    import skelcl_gb300 as S
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # barrier + max over ranks only
+        dist.init_process_group("gloo", init_method="env://")
+    S.init(local_rank if world > 1 else 0)
+    hbm_peak, bf16_peak, peak_kind = peaks()
+
+    # ---- headline: scan + map over 2^28 int32 ------------------------------------
+    x = oracle.mod_i32(N_SCAN, 0, 1001)
+    scan = S.Program(S.KIND_SCAN, "int func(int x, int y){ return x+y; }", ["int"], identity="0")
+    mod = S.Program(S.KIND_MAP, "int func(int x){ return x % 7919; }", ["int", "int"])
+    dx = S.DeviceArray.from_numpy(x)
+    dy = S.DeviceArray(N_SCAN, np.int32)
+
+    ev = [S.Event() for _ in range(3)]
+    per_kernel = {"scan": [], "map": []}
+
+    def step():
+        scan.launch([dx, dy], n=N_SCAN, flags=S.SHAPE_INCLUSIVE)
+        mod.launch([dy, dy], n=N_SCAN)
+
+    def step_events():
+        ev[0].record()
+        scan.launch([dx, dy], n=N_SCAN, flags=S.SHAPE_INCLUSIVE)
+        ev[1].record()
+        mod.launch([dy, dy], n=N_SCAN)
+        ev[2].record()
+
+    for _ in range(args.warmup):
+        step()
+    S.sync()
+    # correctness of the measured configuration (bit-exact vs the oracle, sampled)
+    got = dy.to_numpy()
+    ref = oracle.scan_incl_mod_i32_mt(x, MOD)
+    parity = bool(np.array_equal(got, ref))
+    del got, ref
+
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    launches0 = S.launch_count()
+    t0 = S.Event()
+    t1 = S.Event()
+    S.sync()
+    evs = [[S.Event() for _ in range(3)] for _ in range(args.steps)]
+    t0.record()
+    for k in range(args.steps):
+        ev[:] = evs[k]
+        step_events()
+    t1.record()
+    S.sync()
+    ms_total = t0.elapsed_ms(t1)
+    for e in evs:
+        per_kernel["scan"].append(e[0].elapsed_ms(e[1]))
+        per_kernel["map"].append(e[1].elapsed_ms(e[2]))
+    launches = S.launch_count() - launches0
+    clocks = sampler.stop()
+    ms_step = ms_total / args.steps
+    if dist:
+        import torch
+        t = torch.tensor([ms_step], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * (BYTES_SCAN + BYTES_MAP) / (ms_step * 1e-3) / 1e9
+
+    scan_ms = statistics.mean(per_kernel["scan"])
+    map_ms = statistics.mean(per_kernel["map"])
+    dominant = "scan" if scan_ms >= map_ms else "map"
+    dom_ms = max(scan_ms, map_ms)
+    dom_bytes = BYTES_SCAN if dominant == "scan" else BYTES_MAP
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = traffic_table()
+    tkey = {"scan": "scl_scan_k<4>/int32/N=2^28", "map": "scl_map_k<4>/int32/N=2^28"}[dominant]
+
+    # ---- e2e through the C ABI with pinned host buffers -----------------------------
+    import ctypes
+    L = S.lib()
+    hin = ctypes.c_void_p()
+    hout = ctypes.c_void_p()
+    S.check(L.scl_host_alloc(4 * N_SCAN, ctypes.byref(hin)))
+    S.check(L.scl_host_alloc(4 * N_SCAN, ctypes.byref(hout)))
+    ctypes.memmove(hin, x.ctypes.data, 4 * N_SCAN)
+
+    def e2e_step():
+        S.check(L.scl_h2d_async(dx.ptr, hin, 4 * N_SCAN))
+        step()
+        S.check(L.scl_d2h_async(hout, dy.ptr, 4 * N_SCAN))
+
+    e2e_ms = timed(S, e2e_step, max(2, args.steps // 2), 1)
+    e2e_val = (BYTES_SCAN + BYTES_MAP) / (e2e_ms * 1e-3) / 1e9
+    L.scl_host_free(hin)
+    L.scl_host_free(hout)
+    del dx, dy
+
+    line = {
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "GB/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32",
+        "data": "synthetic (SplitMix64 seed 0, uniform {0..1000})",
+        "config": {"workload": "inclusive Scan(int32 +) over 2^28 then Map(x mod 7919)",
+                   "n": N_SCAN, "l2": "inputs (1 GiB) larger than L2; no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "parity": {"bit_exact_vs_oracle": parity},
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1),
+                     "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+                     "peak_source": f"hbm_gbs of {peak_kind}",
+                     "traffic": traffic.get(tkey), "algorithmic_bytes": dom_bytes,
+                     "per_kernel_ms": {"scan": round(scan_ms, 4), "map": round(map_ms, 4)}},
+        "e2e": {"value": round(e2e_val, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * N_SCAN,
+                "d2h_bytes_per_step": 4 * N_SCAN, "ms_per_step": round(e2e_ms, 3)},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(sample=1 << 26)
+    if rank == 0 and not args.headline_only:
+        line["skeletons"] = secondary(S, oracle, hbm_peak, args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def cpu_baseline(sample: int, reps: int = 3):
+    """The oracle's multithreaded scan+mod on a bounded sample (host cores)."""
+    import oracle
+    x = oracle.mod_i32(sample, 0, 1001)
+    out = np.empty_like(x)
+    nt = oracle.threads()
+    oracle.scan_incl_mod_i32_mt(x, MOD, nt, out)
+    ts = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        oracle.scan_incl_mod_i32_mt(x, MOD, nt, out)
+        ts.append(time.perf_counter() - t)
+    sec = statistics.median(ts)
+    return {"value": round(16 * sample / sec / 1e9, 3), "unit": "GB/s", "cores": nt, "kind": "port",
+            "sample": f"2^{sample.bit_length() - 1} int32 (scan+mod fused, two-pass chunked), "
+                      f"median of {reps}"}
+
+
+def secondary(S, oracle, hbm_peak, args):
+    out = {}
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12  # nominal FP32 TFLOP/s (152 SMs x 128 lanes x FMA x 2.07 GHz)
+    # dot product: Zip(mult) then Reduce(add), N = 2^24
+    n = 1 << 24
+    a = oracle.uniform_f32(n, 0, -1.0, 1.0)
+    b = oracle.uniform_f32(n, 1, -1.0, 1.0)
+    zp = S.Program(S.KIND_ZIP, "float func(float x, float y){ return x*y; }", ["float"] * 3)
+    rp = S.Program(S.KIND_REDUCE, "float func(float x, float y){ return x+y; }", ["float"], identity="0")
+    da, db = S.DeviceArray.from_numpy(a), S.DeviceArray.from_numpy(b)
+    dz, dr = S.DeviceArray(n, np.float32), S.DeviceArray(1, np.float32)
+    zms = timed(S, lambda: zp.launch([da, db, dz], n=n), 20, 3)
+    rms = timed(S, lambda: rp.launch([dz, dr], n=n), 20, 3)
+    dot = float(dr.to_numpy()[0])
+    ref = oracle.dot_f64(a, b)
+    out["dot_product_2^24"] = {
+        "zip_GBps": round(12 * n / zms / 1e6, 1), "reduce_GBps": round(4 * n / rms / 1e6, 1),
+        "zip_frac": round(12 * n / zms / 1e6 / hbm_peak, 3),
+        "reduce_frac": round(4 * n / rms / 1e6 / hbm_peak, 3),
+        "rel_err_vs_fp64": abs(dot - ref) / abs(ref),
+        "note": "inputs 128 MiB, about L2 size: figures include L2 reuse across iterations"}
+    del da, db, dz, dr
+
+    # float scan 2^26 and its adjoint (reverse scan of the upstream gradient)
+    n = 1 << 26
+    xf = oracle.uniform_f32(n, 2, -1.0, 1.0)
+    g = oracle.uniform_f32(n, 3, -1.0, 1.0)
+    sp = S.Program(S.KIND_SCAN, "float func(float x, float y){ return x+y; }", ["float"], identity="0.0f")
+    dxf, dg, dyf, dgx = (S.DeviceArray.from_numpy(xf), S.DeviceArray.from_numpy(g),
+                         S.DeviceArray(n, np.float32), S.DeviceArray(n, np.float32))
+    fwd = timed(S, lambda: sp.launch([dxf, dyf], n=n, flags=S.SHAPE_INCLUSIVE), 10, 3)
+    bwd = timed(S, lambda: sp.launch([dg, dgx], n=n, flags=S.SHAPE_INCLUSIVE | S.SHAPE_REVERSE), 10, 3)
+    yf = dyf.to_numpy().astype(np.float64)
+    ref = oracle.scan_f64(xf, inclusive=True)
+    out["float_scan_2^26"] = {
+        "fwd_GBps": round(8 * n / fwd / 1e6, 1), "fwd_frac": round(8 * n / fwd / 1e6 / hbm_peak, 3),
+        "adjoint_GBps": round(8 * n / bwd / 1e6, 1),
+        "fwd_plus_adjoint_over_fwd": round((fwd + bwd) / fwd, 3),
+        "max_abs_err_vs_fp64": float(np.abs(yf - ref).max()),
+        "max_abs_prefix": float(np.abs(ref).max())}
+    del dxf, dg, dyf, dgx, yf, ref
+
+    # MapOverlap 8192^2, R = 5 Gaussian, both paddings
+    rows = cols = 8192
+    img = oracle.uniform_f32(rows * cols, 5, 0.0, 255.0)
+    w = oracle.gaussian_weights(5, 2.0)
+    src = ("float func(input_matrix_t img, __global float* w) { float s = 0.0f;"
+           " for (int dy = -5; dy <= 5; ++dy) for (int dx = -5; dx <= 5; ++dx)"
+           "  s += getData(img, dx, dy) * w[(dy + 5) * 11 + (dx + 5)]; return s; }")
+    di, do, dw = S.DeviceArray.from_numpy(img), S.DeviceArray(rows * cols, np.float32), S.DeviceArray.from_numpy(w.ravel())
+    mo = {}
+    for name, pad in (("neutral", S.PAD_NEUTRAL), ("nearest", S.PAD_NEAREST)):
+        p = S.Program(S.KIND_MAPOVERLAP, src, ["float", "float"], overlap_range=5, padding=pad, neutral="0")
+        ms = timed(S, lambda: p.launch([di, do], rows=rows, cols=cols, extra=S.buffer(dw)), 10, 3)
+        gbps = 8 * rows * cols / ms / 1e6
+        tflops = 242 * rows * cols / ms / 1e9
+        mo[name] = {"GBps": round(gbps, 1), "hbm_frac": round(gbps / hbm_peak, 3),
+                    "TFLOPs": round(tflops, 2), "fp32_frac_nominal": round(tflops / fp32_peak, 3),
+                    "variant": p.last_variant}
+    out["mapoverlap_8192^2_R5"] = mo
+    del di, do, dw
+
+    # AllPairs 8192x4096 . 4096x8192 (mult/add), and Manhattan 4096x256 . 256x4096
+    M, K, N = 8192, 4096, 8192
+    A = oracle.normal_f32(M * K, 7)
+    B = oracle.normal_f32(K * N, 8)
+    ap = S.Program(S.KIND_ALLPAIRS, "float func(float x, float y){ return x+y; }", ["float"] * 3,
+                   source2="float func(float x, float y){ return x*y; }", identity="0")
+    dA, dB, dP = S.DeviceArray.from_numpy(A), S.DeviceArray.from_numpy(B), S.DeviceArray(M * N, np.float32)
+    res = {}
+    for name, var in (("fp32_simt", S.VARIANT_SIMT), ("auto", S.VARIANT_AUTO)):
+        ms = timed(S, lambda: ap.launch([dA, dB, dP], rows=M, cols=N, dim=K, tuning=S.Tuning(variant=var)), 3, 1)
+        P = dP.to_numpy().reshape(M, N)
+        rows_chk = np.arange(0, M, M // 16)
+        ref = oracle.gemm_f64(A.reshape(M, K)[rows_chk], B.reshape(K, N))
+        err = np.abs(P[rows_chk].astype(np.float64) - ref)
+        res[name] = {"ms": round(ms, 3), "TFLOPs": round(2 * M * N * K / ms / 1e9, 2),
+                     "variant": ap.last_variant,
+                     "max_rel_err_vs_fp64": float((err / np.maximum(np.abs(ref), 1e-3)).max()),
+                     "max_err_over_max_abs": float(err.max() / np.abs(ref).max())}
+    out["allpairs_8192x4096x8192"] = res
+    del dA, dB, dP, A, B
+    Ml, Kl, Nl = 4096, 256, 4096
+    L_ = oracle.normal_f32(Ml * Kl, 10)
+    R_ = oracle.normal_f32(Kl * Nl, 11)
+    man = S.Program(S.KIND_ALLPAIRS, "float func(float x, float y){ return x+y; }", ["float"] * 3,
+                    source2="float func(float x, float y){ return fabs(x-y); }", identity="0")
+    dL, dR, dM = S.DeviceArray.from_numpy(L_), S.DeviceArray.from_numpy(R_), S.DeviceArray(Ml * Nl, np.float32)
+    ms = timed(S, lambda: man.launch([dL, dR, dM], rows=Ml, cols=Nl, dim=Kl), 5, 2)
+    out["manhattan_4096x256x4096"] = {"ms": round(ms, 3),
+                                       "Gpairops": round(Ml * Nl * Kl / ms / 1e6, 1),
+                                       "TFLOPs_3flop": round(3 * Ml * Nl * Kl / ms / 1e9, 2),
+                                       "fp32_frac_nominal": round(3 * Ml * Nl * Kl / ms / 1e9 / fp32_peak, 3)}
+    return out
+
+
+def run_reference(args):
+    """CPU restatement of the same workload on the host cores (the reference
+    itself cannot run here: it needs an OpenCL platform and libclang)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    n = 1 << 26  # bounded sample per step: 1/4 of the 2^28 workload
+    x = oracle.mod_i32(n, 0, 1001)
+    out = np.empty_like(x)
+    nt = oracle.threads()
+    for _ in range(args.warmup):
+        oracle.scan_incl_mod_i32_mt(x, MOD, nt, out)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.scan_incl_mod_i32_mt(x, MOD, nt, out)
+    sec = (time.perf_counter() - t) / args.steps
+    val = 16 * n / sec / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": "GB/s",
+            "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(sec * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (SplitMix64 seed 0)",
+            "config": {"workload": "inclusive Scan(int32 +) then Map(x mod 7919)",
+                       "sample": "2^26 of the 2^28 elements per step"},
+            "cpu_baseline": {"value": round(val, 3), "unit": "GB/s", "cores": nt, "kind": "port",
+                             "sample": "2^26 int32 per step, scan+mod fused (two-pass chunked)"},
+            "e2e": {"value": round(val, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "SkelCL itself needs an OpenCL platform + libclang (absent); this is the oracle port"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--headline-only", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 1:
+        args.warmup = 1
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

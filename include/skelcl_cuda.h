@@ -1,0 +1,243 @@
+/*
+ * skelcl_cuda.h -- the C ABI between the SkelCL C++ headers and the GB300
+ * (sm_103a) runtime in libskelcl_cuda.so.
+ *
+ * The SkelCL header templates (include/SkelCL/*.h) call only these entry
+ * points.  Every function returns an int status (SCL_OK == 0); the message of
+ * the last failure on the calling thread is returned by scl_last_error_string().
+ * Arguments are plain pointers and sizes: no C++ or torch types cross this
+ * boundary, so ctypes / cffi / JNI / cgo bind it directly.
+ *
+ * Each entry point names the reference interface it replaces (paths are
+ * relative to the SkelCL source tree).
+ */
+#ifndef SKELCL_CUDA_H_
+#define SKELCL_CUDA_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SCL_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum scl_status {
+  SCL_OK = 0,
+  SCL_ERR_ARG = 1,         /* bad argument: null pointer, size, arg list   */
+  SCL_ERR_OOM = 2,         /* device allocation failed                     */
+  SCL_ERR_COMPILE = 3,     /* user source did not splice or compile        */
+  SCL_ERR_LAUNCH = 4,      /* kernel launch failed                         */
+  SCL_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up           */
+  SCL_ERR_CUDA = 6,        /* any other CUDA runtime / driver error        */
+  SCL_ERR_NOT_INIT = 7,    /* scl_init() was not called                    */
+  SCL_ERR_UNSUPPORTED = 8  /* valid request this build does not implement  */
+};
+
+/* ---- skeleton kinds (one program per skeleton object) ------------------- */
+enum scl_kind {
+  SCL_KIND_MAP = 1,             /* Tout f(Tin, extra...)        MapDef.h:75-195    */
+  SCL_KIND_MAP_VOID = 2,        /* void f(Tin, extra...)        MapDef.h:219-332   */
+  SCL_KIND_MAP_INDEX = 3,       /* Tout f(Index, extra...)      MapDef.h:335-469   */
+  SCL_KIND_MAP_INDEX_VOID = 4,  /* void f(Index, extra...)      src/Map.cpp:50-95  */
+  SCL_KIND_MAP_POINT = 5,       /* Tout f(IndexPoint, extra...) MapDef.h:533-684   */
+  SCL_KIND_MAP_POINT_VOID = 6,  /* void f(IndexPoint, extra...) src/Map.cpp:97-150 */
+  SCL_KIND_ZIP = 7,             /* Tout f(Tl, Tr, extra...)     ZipDef.h:70-206    */
+  SCL_KIND_ZIP_VOID = 8,        /* void f(Tl, Tr, extra...)     ZipDef.h:287-397   */
+  SCL_KIND_REDUCE = 9,          /* T f(T, T, extra...)          ReduceDef.h:79-275 */
+  SCL_KIND_SCAN = 10,           /* T f(T, T, extra...)          ScanDef.h:70-297   */
+  SCL_KIND_MAPOVERLAP = 11,     /* Tout f(input_matrix_t, ...)  MapOverlapDef.h:71-279 */
+  SCL_KIND_ALLPAIRS = 12,       /* reduce + zip pair            AllPairsDef.h:77-91,213-280 */
+  SCL_KIND_ALLPAIRS_GENERIC = 13 /* Tout f(lmatrix_t*, rmatrix_t*, dim, ...) AllPairsDef.h:93-107,283-344 */
+};
+
+/* MapOverlap padding modes (include/SkelCL/detail/Padding.h:47-50). */
+enum scl_padding { SCL_PAD_NEUTRAL = 0, SCL_PAD_NEAREST = 1 };
+
+/* Program description.  Field meaning follows the reference constructors:
+ * `source`/`func` are the user source and function name (Map.h:141-142,
+ * Zip.h:96-120, Reduce.h:95-120, Scan.h:80-99, MapOverlap.h:119-140,
+ * AllPairs.h:127-140).  For SCL_KIND_ALLPAIRS `source`/`func` are the
+ * Reduce's and `source2`/`func2` the Zip's.  `type_names` are the OpenCL C
+ * spellings of the element types in skeleton order (Tin, Tout / Tl, Tr, Tout /
+ * T), as detail::util::typeToString produces them (detail/Util.h:81-98). */
+typedef struct scl_program_desc {
+  int kind;                       /* enum scl_kind */
+  const char* source;             /* user source (OpenCL C)                  */
+  const char* func;               /* user function name, "func" if NULL      */
+  const char* source2;            /* AllPairs: the Zip's source              */
+  const char* func2;              /* AllPairs: the Zip's function name       */
+  const char* identity;           /* Reduce/Scan/AllPairs identity, "0"      */
+  const char* type_names[3];      /* element types                           */
+  int n_types;
+  int overlap_range;              /* MapOverlap radius R                     */
+  int padding;                    /* enum scl_padding                        */
+  const char* neutral;            /* MapOverlap neutral element (C literal)  */
+  const char* common_source;      /* CommonDefinitions (src/Source.cpp:118-126) */
+  uint32_t flags;                 /* SCL_PROG_* below                        */
+} scl_program_desc;
+
+/* Program flags. */
+#define SCL_PROG_NO_F64_CARRY 0x1u  /* keep float carries in float            */
+
+typedef struct scl_program scl_program;
+
+/* Launch shape.  Only the fields a skeleton uses are read. */
+typedef struct scl_shape {
+  uint64_t n;            /* element count (Map/Zip/Reduce/Scan, flat length)  */
+  uint64_t rows;         /* matrix rows (MapOverlap, Map<IndexPoint>, AllPairs output) */
+  uint64_t cols;         /* matrix columns                                     */
+  uint64_t dim;          /* AllPairs inner dimension                          */
+  uint64_t offset;       /* Map<Index>: first index; Map<IndexPoint>: row offset */
+  const uint64_t* seg_offsets; /* segmented launches: DEVICE array, n_segments+1 */
+  uint64_t n_segments;   /* 0 = not segmented                                 */
+  uint32_t flags;        /* SCL_SHAPE_* below                                 */
+  uint32_t reserved;
+} scl_shape;
+
+#define SCL_SHAPE_INCLUSIVE 0x1u  /* Scan: inclusive instead of exclusive     */
+#define SCL_SHAPE_REVERSE   0x2u  /* Scan: scan from the end (adjoint of Scan) */
+
+/* Launch tuning; NULL means "defaults or autotuned".  Zero fields keep their
+ * default.  workgroup mirrors Skeleton::setWorkGroupSize (src/Skeleton.cpp:75-78). */
+typedef struct scl_tuning {
+  uint32_t workgroup;    /* threads per block                                 */
+  uint32_t items;        /* vector rows per thread (Map/Zip/Reduce/Scan)       */
+  uint32_t tile_w;       /* MapOverlap tile width / AllPairs tile             */
+  uint32_t tile_h;       /* MapOverlap rows per thread                        */
+  uint32_t variant;      /* SCL_VARIANT_*                                     */
+  uint32_t spin_limit;   /* bounded-wait polls before SCL_ERR_TIMEOUT, 0 = default */
+} scl_tuning;
+
+#define SCL_VARIANT_AUTO 0u
+#define SCL_VARIANT_SIMPLE 1u     /* one element per thread (reference shape) */
+#define SCL_VARIANT_VECTOR 2u     /* grid-stride 128-bit vectorised           */
+#define SCL_VARIANT_SIMT 3u       /* AllPairs: FP32 SIMT register tiles       */
+#define SCL_VARIANT_TC3XBF16 4u   /* AllPairs: tcgen05 3xBF16 contraction     */
+#define SCL_VARIANT_TMA 5u        /* MapOverlap: TMA-staged tile              */
+#define SCL_VARIANT_LDST 6u       /* MapOverlap: cooperative-load tile        */
+
+/* ---- extra-argument blob ----------------------------------------------- *
+ * The extra arguments of a skeleton call are packed in call order into one
+ * blob of records { uint32 kind; uint32 size; payload padded to 8 bytes }.
+ * Kinds follow detail::kernelUtil::setKernelArgs (detail/KernelUtil.h:132-245):
+ *   SCL_ARG_VALUE   payload = `size` raw bytes of a scalar / struct
+ *   SCL_ARG_BUFFER  payload = device pointer (Vector argument)
+ *   SCL_ARG_MATRIX  payload = device pointer, uint32 column count (Matrix)
+ *   SCL_ARG_LOCAL   payload = uint64 byte count of __local memory (Local)   */
+enum scl_arg_kind {
+  SCL_ARG_VALUE = 1,
+  SCL_ARG_BUFFER = 2,
+  SCL_ARG_MATRIX = 3,
+  SCL_ARG_LOCAL = 4
+};
+
+/* ---- runtime: replaces skelcl::init / terminate (include/SkelCL/SkelCL.h:144-207,
+ *      src/SkelCL.cpp:51-85, src/DeviceList.cpp:82-123, src/Device.cpp:95-122) */
+int scl_init(int device);
+int scl_terminate(void);
+int scl_is_initialized(void);
+int scl_device_info(int* sm_count, size_t* global_mem, char* name, size_t name_cap);
+const char* scl_last_error_string(void);
+int scl_abi_version(void);
+
+/* ---- memory: replaces detail::DeviceBuffer and Device::enqueueWrite/Read/Copy
+ *      (src/DeviceBuffer.cpp:60-135, src/Device.cpp:169-330).  All copies are
+ *      ordered on the library stream; scl_h2d/scl_d2h return after the copy is
+ *      complete (host buffers may be reused), the _async forms do not. */
+int scl_alloc(size_t bytes, void** dptr);
+int scl_free(void* dptr);
+int scl_h2d(void* dst, const void* src, size_t bytes);
+int scl_d2h(void* dst, const void* src, size_t bytes);
+int scl_d2d(void* dst, const void* src, size_t bytes);
+int scl_h2d_async(void* dst, const void* src, size_t bytes);
+int scl_d2h_async(void* dst, const void* src, size_t bytes);
+int scl_memset(void* dst, int value, size_t bytes);
+int scl_host_alloc(size_t bytes, void** hptr); /* pinned host memory */
+int scl_host_free(void* hptr);
+int scl_sync(void);                 /* wait for the stream; reports device-side errors */
+
+/* ---- events: replaces detail::Event (src/Event.cpp) and the profiling queue */
+typedef struct scl_event scl_event;
+int scl_event_create(scl_event** ev);
+int scl_event_record(scl_event* ev);
+int scl_event_elapsed_ms(scl_event* start, scl_event* stop, float* ms);
+int scl_event_destroy(scl_event* ev);
+
+/* ---- programs: replaces detail::Program + stooling rewriting
+ *      (src/Program.cpp:83-250, include/SkelCL/detail/Program.h:61-132,
+ *      libraries/stooling/src/SourceCode.cpp:98-263).  Splices the user
+ *      function into the sm_103a skeleton template and compiles it with NVRTC.
+ *      On failure `log` (if given) receives the splice / NVRTC log. */
+int scl_program_build(const scl_program_desc* desc, scl_program** out,
+                      char* log, size_t log_cap);
+int scl_program_release(scl_program* prog);
+/* Splice and compile only (no device needed, nothing loaded): the check that
+ * a user source is accepted, usable before scl_init(). */
+int scl_program_compile(const scl_program_desc* desc, char* log, size_t log_cap);
+/* Number of extra (non-skeleton) parameters the user function declares. */
+int scl_program_extra_count(const scl_program* prog, int* count);
+/* Hex SHA-1 of the assembled source (the program-cache key, src/Util.cpp:159-180). */
+int scl_program_hash(const scl_program* prog, char* out41);
+/* Splice-only dry run: writes the generated CUDA source, compiles nothing. */
+int scl_program_source(const scl_program_desc* desc, char* out, size_t cap,
+                       size_t* needed);
+
+/* SHA-1 of arbitrary bytes as 40 hex characters + NUL (util::hash). */
+int scl_sha1_hex(const void* data, size_t bytes, char* out41);
+
+/* ---- launches: replace the per-skeleton execute() bodies.  `buffers` holds
+ *      device pointers in skeleton order:
+ *        map:        {in, out}      (void map: {in}; Index maps: {out} / {})
+ *        zip:        {left, right, out}   (void zip: {left, right})
+ *        reduce:     {in, out}      out receives 1 element (n_segments elements
+ *                                   for a segmented reduce)
+ *        scan:       {in, out}
+ *        mapoverlap: {in, out}      rows x cols, row-major
+ *        allpairs:   {left, right, out}  left rows x dim, right dim x cols
+ *      All launches are asynchronous on the library stream. */
+int scl_launch_map(scl_program* prog, const scl_shape* shape,
+                   void* const* buffers, const void* extra, size_t extra_bytes,
+                   const scl_tuning* tuning);
+int scl_launch_zip(scl_program* prog, const scl_shape* shape,
+                   void* const* buffers, const void* extra, size_t extra_bytes,
+                   const scl_tuning* tuning);
+int scl_launch_reduce(scl_program* prog, const scl_shape* shape,
+                      void* const* buffers, const void* extra,
+                      size_t extra_bytes, const scl_tuning* tuning);
+int scl_launch_scan(scl_program* prog, const scl_shape* shape,
+                    void* const* buffers, const void* extra, size_t extra_bytes,
+                    const scl_tuning* tuning);
+int scl_launch_mapoverlap(scl_program* prog, const scl_shape* shape,
+                          void* const* buffers, const void* extra,
+                          size_t extra_bytes, const scl_tuning* tuning);
+int scl_launch_allpairs(scl_program* prog, const scl_shape* shape,
+                        void* const* buffers, const void* extra,
+                        size_t extra_bytes, const scl_tuning* tuning);
+
+/* Variant the last launch of `prog` used (SCL_VARIANT_*). */
+int scl_program_last_variant(const scl_program* prog, uint32_t* variant);
+/* Kernels this library launched since scl_init (all programs). */
+int scl_launch_count(uint64_t* count);
+
+/* ---- CUDA graphs (no reference counterpart: skeleton sequences captured
+ *      from the library stream and replayed with one launch). */
+typedef struct scl_graph scl_graph;
+int scl_graph_begin(void);
+int scl_graph_end(scl_graph** graph);
+int scl_graph_launch(scl_graph* graph);
+int scl_graph_destroy(scl_graph* graph);
+
+/* ---- test hook for the bounded-wait machinery: launches one block that
+ *      waits on a flag nothing sets, with at most `polls` polls, and stores
+ *      the kernel's status in *status (SCL_OK or SCL_ERR_TIMEOUT).  Faults
+ *      nothing and returns when the wait gives up. */
+int scl_debug_bounded_wait(uint32_t polls, int* status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SKELCL_CUDA_H_ */

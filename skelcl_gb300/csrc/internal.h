@@ -1,0 +1,140 @@
+// Internal declarations shared by the libskelcl_cuda.so translation units.
+#ifndef SKELCL_GB300_INTERNAL_H_
+#define SKELCL_GB300_INTERNAL_H_
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "skelcl_cuda.h"
+
+namespace scl {
+
+// ---- error reporting ------------------------------------------------------
+int fail(int status, const std::string& msg);  // records msg, returns status
+int cuda_fail(cudaError_t e, const char* what);
+int cu_fail(CUresult r, const char* what);
+
+#define SCL_CUDA(call)                                  \
+  do {                                                  \
+    cudaError_t scl_e_ = (call);                        \
+    if (scl_e_ != cudaSuccess) return ::scl::cuda_fail(scl_e_, #call); \
+  } while (0)
+#define SCL_CU(call)                                    \
+  do {                                                  \
+    CUresult scl_r_ = (call);                           \
+    if (scl_r_ != CUDA_SUCCESS) return ::scl::cu_fail(scl_r_, #call); \
+  } while (0)
+
+// ---- driver entry points (resolved through the runtime, no -lcuda) --------
+struct Driver {
+  CUresult (*cuModuleLoadData)(CUmodule*, const void*) = nullptr;
+  CUresult (*cuModuleUnload)(CUmodule) = nullptr;
+  CUresult (*cuModuleGetFunction)(CUfunction*, CUmodule, const char*) = nullptr;
+  CUresult (*cuModuleGetGlobal)(CUdeviceptr*, size_t*, CUmodule, const char*) = nullptr;
+  CUresult (*cuFuncSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
+  CUresult (*cuFuncGetAttribute)(int*, CUfunction_attribute, CUfunction) = nullptr;
+  CUresult (*cuLaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned,
+                             unsigned, unsigned, unsigned, CUstream, void**,
+                             void**) = nullptr;
+  CUresult (*cuOccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int,
+                                                          size_t) = nullptr;
+  CUresult (*cuFuncGetParamInfo)(CUfunction, size_t, size_t*, size_t*) = nullptr;
+  CUresult (*cuTensorMapEncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
+                                     void*, const cuuint64_t*, const cuuint64_t*,
+                                     const cuuint32_t*, const cuuint32_t*,
+                                     CUtensorMapInterleave, CUtensorMapSwizzle,
+                                     CUtensorMapL2promotion,
+                                     CUtensorMapFloatOOBfill) = nullptr;
+  CUresult (*cuGetErrorString)(CUresult, const char**) = nullptr;
+};
+
+// ---- global runtime state -------------------------------------------------
+struct Runtime {
+  bool initialized = false;
+  int device = 0;
+  int sm_count = 0;
+  int cc_major = 0, cc_minor = 0;
+  size_t smem_optin = 0;
+  size_t global_mem = 0;
+  std::string name;
+  cudaStream_t stream = nullptr;
+  unsigned int* dev_err = nullptr;   // device-side status word
+  unsigned int* host_err = nullptr;  // pinned mirror
+  uint64_t launches = 0;
+  bool capturing = false;
+  Driver drv;
+};
+Runtime& rt();
+int require_init();
+
+// ---- splicer ----------------------------------------------------------------
+enum class ParamKind { Value, Buffer, Matrix, Local };
+struct Param {
+  std::string type;   // declared type text (qualifiers kept)
+  std::string name;   // parameter name
+  ParamKind kind = ParamKind::Value;
+  std::string elem;   // Matrix: element type spelling; Local: pointee type
+};
+struct FuncSig {
+  std::string ret;
+  std::vector<Param> params;
+  size_t def_begin = 0;  // offset of the return type in the source
+  size_t def_end = 0;    // one past the closing brace of the body
+};
+bool parse_function(const std::string& src, const std::string& name, FuncSig* sig,
+                    std::string* err);
+std::string rename_identifier(const std::string& src, const std::string& from,
+                              const std::string& to);
+bool source_uses_workitem(const std::string& src);
+std::string sha1_hex(const void* data, size_t n);
+
+// ---- programs -----------------------------------------------------------------
+struct Kernel {
+  CUfunction fn = nullptr;
+  std::string name;
+};
+
+struct Workspace {  // per-program scratch (reduce partials, scan tile status)
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace scl
+
+struct scl_program {
+  int kind = 0;
+  std::string hash;
+  std::string source;                       // generated CUDA source
+  std::vector<scl::Param> extra;            // user extra params (Reduce's then Zip's for AllPairs)
+  size_t n_reduce_extra = 0;                // AllPairs: how many of `extra` belong to the Reduce
+  std::vector<size_t> type_sizes;           // sizeof SCL_TYPE_n (read from the module)
+  size_t carry_size = 0;                    // sizeof SCL_CARRY_T (Reduce / Scan)
+  std::vector<std::string> type_names;
+  bool uses_workitem = false;
+  bool f64_carry = false;
+  bool tc_eligible = false;                 // AllPairs: zip == x*y, reduce == x+y, id 0, float
+  int overlap_range = 0;
+  int padding = 0;
+  CUmodule module = nullptr;
+  std::map<std::string, scl::Kernel> kernels;  // by template name expression
+  scl::Workspace ws;
+  uint32_t last_variant = 0;
+};
+
+namespace scl {
+CUfunction find_kernel(scl_program* p, const std::string& name);
+int ensure_workspace(scl_program* p, size_t bytes);
+// Autotuner lookup/store; returns false when nothing is cached.
+bool tune_lookup(const std::string& key, scl_tuning* out);
+void tune_store(const std::string& key, const scl_tuning& t);
+bool autotune_enabled();
+}  // namespace scl
+
+#endif  // SKELCL_GB300_INTERNAL_H_

@@ -1,0 +1,468 @@
+// Skeleton launches: the GB300 counterparts of the reference's execute()
+// bodies (MapDef.h:118-166, ZipDef.h:119-173, ReduceDef.h:164-245,
+// ScanDef.h:178-259, MapOverlapDef.h:116-178, AllPairsDef.h:146-210) and of
+// the argument marshalling in detail::kernelUtil::setKernelArgs
+// (include/SkelCL/detail/KernelUtil.h:132-245).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "internal.h"
+
+// tcgen05 contraction (allpairs_tc.cu)
+namespace scl {
+int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uint32_t N,
+                       uint32_t K, cudaStream_t stream, uint32_t spin_limit, unsigned int* err);
+bool allpairs_tc_supported(uint32_t M, uint32_t N, uint32_t K, const void* A, const void* B,
+                           const void* P);
+}  // namespace scl
+
+namespace scl {
+namespace {
+
+constexpr uint32_t kDefaultSpin = 1u << 22;  // polls; ~0.1-1 s with back-off
+
+struct ArgPack {
+  std::vector<void*> ptrs;
+  uint32_t vals[64];  // storage for values built here (Local offsets)
+  int nvals = 0;
+  size_t local_bytes = 0;
+};
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+const char* kind_name(uint32_t k) {
+  switch (k) {
+    case SCL_ARG_VALUE: return "scalar";
+    case SCL_ARG_BUFFER: return "Vector";
+    case SCL_ARG_MATRIX: return "Matrix";
+    case SCL_ARG_LOCAL: return "Local";
+    default: return "unknown";
+  }
+}
+
+// Walks the blob against program parameters [first, first+count) and appends
+// kernel-parameter pointers.  `fixed` = number of skeleton kernel params
+// before the extras (for the parameter-size check).
+int pack_extra(scl_program* p, CUfunction fn, size_t fixed, const unsigned char* blob,
+               size_t bytes, ArgPack* pack) {
+  size_t off = 0;
+  size_t kparam = fixed;  // kernel parameter index
+  const size_t count = p->extra.size();
+  for (size_t i = 0; i < count; ++i) {
+    if (off + 8 > bytes)
+      return fail(SCL_ERR_ARG, "too few extra arguments: the user function declares " +
+                                   std::to_string(count) + ", the call passes " + std::to_string(i));
+    uint32_t kind, size;
+    std::memcpy(&kind, blob + off, 4);
+    std::memcpy(&size, blob + off + 4, 4);
+    const unsigned char* payload = blob + off + 8;
+    size_t rec = 8 + ((size + 7u) & ~7u);
+    if (off + rec > bytes) return fail(SCL_ERR_ARG, "truncated extra-argument record");
+    const Param& prm = p->extra[i];
+    auto mismatch = [&](const char* want) {
+      return fail(SCL_ERR_ARG, "extra argument " + std::to_string(i) + " ('" + prm.name +
+                                   "'): the user function expects " + want + ", the call passes " +
+                                   kind_name(kind));
+    };
+    switch (prm.kind) {
+      case ParamKind::Value: {
+        if (kind != SCL_ARG_VALUE) return mismatch("a scalar");
+        if (rt().drv.cuFuncGetParamInfo && fn) {
+          size_t po = 0, ps = 0;
+          if (rt().drv.cuFuncGetParamInfo(fn, kparam, &po, &ps) == CUDA_SUCCESS && ps != size)
+            return fail(SCL_ERR_ARG, "extra argument " + std::to_string(i) + " ('" + prm.name +
+                                         "'): " + std::to_string(size) + " bytes passed, " +
+                                         std::to_string(ps) + " expected");
+        }
+        pack->ptrs.push_back(const_cast<unsigned char*>(payload));
+        ++kparam;
+        break;
+      }
+      case ParamKind::Buffer: {
+        if (kind == SCL_ARG_BUFFER) {
+          pack->ptrs.push_back(const_cast<unsigned char*>(payload));
+          ++kparam;
+        } else if (kind == SCL_ARG_MATRIX) {
+          // reference form: `__global T* m, uint m_col_count` (KernelUtil.h:189)
+          if (i + 1 >= count || p->extra[i + 1].kind != ParamKind::Value)
+            return mismatch("a pointer followed by a column count");
+          pack->ptrs.push_back(const_cast<unsigned char*>(payload));
+          pack->ptrs.push_back(const_cast<unsigned char*>(payload + 8));
+          kparam += 2;
+          ++i;  // the column-count parameter is consumed
+        } else {
+          return mismatch("a Vector");
+        }
+        break;
+      }
+      case ParamKind::Matrix: {
+        if (kind != SCL_ARG_MATRIX) return mismatch("a Matrix");
+        pack->ptrs.push_back(const_cast<unsigned char*>(payload));
+        pack->ptrs.push_back(const_cast<unsigned char*>(payload + 8));
+        kparam += 2;
+        break;
+      }
+      case ParamKind::Local: {
+        if (kind != SCL_ARG_LOCAL) return mismatch("Local memory");
+        uint64_t lb = 0;
+        std::memcpy(&lb, payload, 8);
+        size_t o = (pack->local_bytes + 15) & ~(size_t)15;
+        if (pack->nvals >= 64) return fail(SCL_ERR_ARG, "too many Local arguments");
+        pack->vals[pack->nvals] = (uint32_t)o;
+        pack->ptrs.push_back(&pack->vals[pack->nvals]);
+        ++pack->nvals;
+        pack->local_bytes = o + lb;
+        ++kparam;
+        break;
+      }
+    }
+    off += rec;
+  }
+  if (off != bytes)
+    return fail(SCL_ERR_ARG, "too many extra arguments: the user function declares " +
+                                 std::to_string(count));
+  return SCL_OK;
+}
+
+int launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, ArgPack& pack) {
+  if (smem > 48 * 1024) {
+    CUresult r = rt().drv.cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                             (int)smem);
+    if (r != CUDA_SUCCESS) return cu_fail(r, "cuFuncSetAttribute(max dynamic smem)");
+  }
+  CUresult r = rt().drv.cuLaunchKernel(fn, grid.x, grid.y, grid.z, block.x, block.y, block.z,
+                                       (unsigned)smem, (CUstream)rt().stream,
+                                       pack.ptrs.empty() ? nullptr : pack.ptrs.data(), nullptr);
+  if (r != CUDA_SUCCESS) return cu_fail(r, "cuLaunchKernel");
+  ++rt().launches;
+  return SCL_OK;
+}
+
+int max_resident_blocks(CUfunction fn, int block, size_t smem) {
+  int per_sm = 0;
+  if (rt().drv.cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem) != CUDA_SUCCESS ||
+      per_sm < 1)
+    per_sm = 1;
+  return per_sm * rt().sm_count;
+}
+
+int vec_width(size_t s0, size_t s1 = 1, size_t s2 = 1) {
+  size_t s = std::max(s0, std::max(s1, s2));
+  if (s <= 16 && 16 % s == 0 && 16 % s0 == 0 && 16 % s1 == 0 && 16 % s2 == 0) return (int)(16 / s);
+  return 1;
+}
+
+uint32_t pick_block(const scl_tuning* t, uint32_t dflt) {
+  uint32_t b = (t && t->workgroup) ? t->workgroup : dflt;
+  if (b > 1024) b = 1024;
+  if (b == 0) b = dflt;
+  return b;
+}
+
+uint32_t spin_of(const scl_tuning* t) { return (t && t->spin_limit) ? t->spin_limit : kDefaultSpin; }
+
+int check_prog(scl_program* p, std::initializer_list<int> kinds) {
+  if (int st = require_init()) return st;
+  if (!p) return fail(SCL_ERR_ARG, "null program");
+  for (int k : kinds)
+    if (p->kind == k) return SCL_OK;
+  return fail(SCL_ERR_ARG, "program kind " + std::to_string(p->kind) + " does not match this launch");
+}
+
+}  // namespace
+}  // namespace scl
+
+using namespace scl;
+
+// ---- Map / Zip ----------------------------------------------------------------
+extern "C" int scl_launch_map(scl_program* p, const scl_shape* sh, void* const* bufs,
+                              const void* extra, size_t extra_bytes, const scl_tuning* tu) {
+  if (int st = check_prog(p, {SCL_KIND_MAP, SCL_KIND_MAP_VOID, SCL_KIND_MAP_INDEX,
+                              SCL_KIND_MAP_INDEX_VOID, SCL_KIND_MAP_POINT,
+                              SCL_KIND_MAP_POINT_VOID, SCL_KIND_ZIP, SCL_KIND_ZIP_VOID}))
+    return st;
+  if (!sh) return fail(SCL_ERR_ARG, "null shape");
+  const int kind = p->kind;
+  const bool point = kind == SCL_KIND_MAP_POINT || kind == SCL_KIND_MAP_POINT_VOID;
+  int nbuf = 0;
+  switch (kind) {
+    case SCL_KIND_MAP: nbuf = 2; break;
+    case SCL_KIND_MAP_VOID: nbuf = 1; break;
+    case SCL_KIND_MAP_INDEX: nbuf = 1; break;
+    case SCL_KIND_MAP_POINT: nbuf = 1; break;
+    case SCL_KIND_ZIP: nbuf = 3; break;
+    case SCL_KIND_ZIP_VOID: nbuf = 2; break;
+    default: nbuf = 0;
+  }
+  if (nbuf && !bufs) return fail(SCL_ERR_ARG, "null buffer list");
+  void* b[3] = {nullptr, nullptr, nullptr};
+  for (int i = 0; i < nbuf; ++i) {
+    b[i] = bufs[i];
+    if (!b[i]) return fail(SCL_ERR_ARG, "null device buffer " + std::to_string(i));
+  }
+  uint64_t n = sh->n, rows = sh->rows, cols = sh->cols, offset = sh->offset;
+  if (point) n = rows * cols;
+  if (n == 0) return SCL_OK;
+  bool simple = p->uses_workitem || (tu && tu->variant == SCL_VARIANT_SIMPLE);
+  int aligned = 1;
+  for (int i = 0; i < nbuf; ++i) aligned &= aligned16(b[i]) ? 1 : 0;
+  uint32_t items = (tu && tu->items) ? tu->items : 4;
+  if (items != 1 && items != 2 && items != 4) items = 4;
+  std::string kname = simple ? "scl_map_simple" : "scl_map_k<" + std::to_string(items) + ">";
+  CUfunction fn = find_kernel(p, kname);
+  if (!fn) return fail(SCL_ERR_LAUNCH, "kernel " + kname + " missing from the program");
+
+  ArgPack pack;
+  pack.ptrs.reserve(32);
+  for (int i = 0; i < nbuf; ++i) pack.ptrs.push_back(&b[i]);
+  if (point) {
+    pack.ptrs.push_back(&rows);
+    pack.ptrs.push_back(&cols);
+    pack.ptrs.push_back(&offset);
+  } else {
+    pack.ptrs.push_back(&n);
+    if (kind == SCL_KIND_MAP_INDEX || kind == SCL_KIND_MAP_INDEX_VOID) pack.ptrs.push_back(&offset);
+  }
+  if (!simple) pack.ptrs.push_back(&aligned);
+  const size_t fixed = pack.ptrs.size();
+  if (int st = pack_extra(p, fn, fixed, (const unsigned char*)extra, extra_bytes, &pack)) return st;
+
+  uint32_t wg = pick_block(tu, 256);
+  dim3 grid, block;
+  if (simple) {
+    if (point) {
+      // reference: local = floorPow2(sqrt(wg))^2 (MapDef.h:590-597)
+      uint32_t s = 1;
+      while ((s * 2) * (s * 2) <= wg) s *= 2;
+      block = dim3(s, s, 1);
+      uint64_t gx = (cols + s - 1) / s, gy = (rows + s - 1) / s;
+      if (gx > 0x7fffffffull || gy > 65535) return fail(SCL_ERR_ARG, "matrix too large for the one-thread-per-element shape");
+      grid = dim3((unsigned)gx, (unsigned)gy, 1);
+    } else {
+      block = dim3(wg, 1, 1);
+      uint64_t g = (n + wg - 1) / wg;
+      if (g > 0x7fffffffull) return fail(SCL_ERR_ARG, "vector too large for the one-thread-per-element shape");
+      grid = dim3((unsigned)g, 1, 1);
+    }
+    p->last_variant = SCL_VARIANT_SIMPLE;
+  } else {
+    const int maxb = max_resident_blocks(fn, (int)wg, pack.local_bytes);
+    if (point) {
+      uint32_t bx = 256;
+      block = dim3(bx, 1, 1);
+      uint64_t gx = (cols + bx - 1) / bx;
+      if (gx > (uint64_t)maxb) gx = (uint64_t)maxb;
+      uint64_t gy = rows;
+      uint64_t cap = std::max<uint64_t>(1, (uint64_t)maxb * 4 / gx);
+      if (gy > cap) gy = cap;
+      if (gy > 65535) gy = 65535;
+      grid = dim3((unsigned)gx, (unsigned)std::max<uint64_t>(gy, 1), 1);
+    } else {
+      size_t s0 = p->type_sizes.size() > 0 ? p->type_sizes[0] : 4;
+      size_t s1 = p->type_sizes.size() > 1 ? p->type_sizes[1] : s0;
+      size_t s2 = p->type_sizes.size() > 2 ? p->type_sizes[2] : s0;
+      int V = (kind == SCL_KIND_MAP_INDEX_VOID) ? 1 : vec_width(s0, s1, s2);
+      uint64_t units = aligned ? (n + V - 1) / V : n;
+      uint64_t g = (units + wg - 1) / wg;
+      if (g > (uint64_t)maxb) g = (uint64_t)maxb;
+      block = dim3(wg, 1, 1);
+      grid = dim3((unsigned)std::max<uint64_t>(g, 1), 1, 1);
+    }
+    p->last_variant = SCL_VARIANT_VECTOR;
+  }
+  return launch(fn, grid, block, pack.local_bytes, pack);
+}
+
+extern "C" int scl_launch_zip(scl_program* p, const scl_shape* sh, void* const* bufs,
+                              const void* extra, size_t extra_bytes, const scl_tuning* tu) {
+  if (int st = check_prog(p, {SCL_KIND_ZIP, SCL_KIND_ZIP_VOID})) return st;
+  return scl_launch_map(p, sh, bufs, extra, extra_bytes, tu);
+}
+
+// ---- Reduce -------------------------------------------------------------------
+extern "C" int scl_launch_reduce(scl_program* p, const scl_shape* sh, void* const* bufs,
+                                 const void* extra, size_t extra_bytes, const scl_tuning* tu) {
+  if (int st = check_prog(p, {SCL_KIND_REDUCE})) return st;
+  if (!sh || !bufs || !bufs[0] || !bufs[1]) return fail(SCL_ERR_ARG, "reduce needs {in, out}");
+  void* in = bufs[0];
+  void* out = bufs[1];
+  uint64_t n = sh->n;
+  const size_t tsz = p->type_sizes[0], csz = p->carry_size ? p->carry_size : tsz;
+  const int V = vec_width(tsz);
+  int aligned = aligned16(in) ? 1 : 0;
+  uint32_t items = (tu && tu->items) ? tu->items : 4;
+  if (items != 1 && items != 2 && items != 4) items = 4;
+  std::string kname = "scl_reduce_k<" + std::to_string(items) + ">";
+  CUfunction fn = find_kernel(p, kname);
+  if (!fn) return fail(SCL_ERR_LAUNCH, "kernel " + kname + " missing");
+  uint32_t wg = pick_block(tu, 256);
+  wg = (wg + 31) / 32 * 32;
+  const int maxb = max_resident_blocks(fn, (int)wg, 0);
+  uint64_t units = aligned ? n / V : n;
+  uint64_t g = units == 0 ? 1 : (units + wg - 1) / wg;
+  if (g > (uint64_t)maxb) g = (uint64_t)maxb;
+  if (g < 1) g = 1;
+  const size_t part_off = 256;
+  if (int st = ensure_workspace(p, part_off + g * csz)) return st;
+  void* partials = (char*)p->ws.ptr + part_off;
+  void* ticket = p->ws.ptr;
+  unsigned int* err = rt().dev_err;
+  ArgPack pack;
+  pack.ptrs = {&in, &out, &n, &aligned, &partials, &ticket, &err};
+  if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
+    return st;
+  p->last_variant = SCL_VARIANT_VECTOR;
+  return launch(fn, dim3((unsigned)g), dim3(wg), 0, pack);
+}
+
+// ---- Scan ---------------------------------------------------------------------
+extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const* bufs,
+                               const void* extra, size_t extra_bytes, const scl_tuning* tu) {
+  if (int st = check_prog(p, {SCL_KIND_SCAN})) return st;
+  if (!sh || !bufs || !bufs[0] || !bufs[1]) return fail(SCL_ERR_ARG, "scan needs {in, out}");
+  void* in = bufs[0];
+  void* out = bufs[1];
+  uint64_t n = sh->n;
+  if (n == 0) return SCL_OK;
+  const size_t tsz = p->type_sizes[0], csz = p->carry_size ? p->carry_size : tsz;
+  const int V = vec_width(tsz);
+  uint32_t R = (tu && tu->items) ? tu->items : 4;
+  if (R != 2 && R != 4) R = 4;
+  const uint64_t tile = (uint64_t)R * 256 * V;
+  const uint64_t tiles = (n + tile - 1) / tile;
+  if (tiles > 0x7fffffffull) return fail(SCL_ERR_ARG, "scan input too large");
+  std::string kname = "scl_scan_k<" + std::to_string(R) + ">";
+  CUfunction fn = find_kernel(p, kname);
+  if (!fn) return fail(SCL_ERR_LAUNCH, "kernel " + kname + " missing");
+  const size_t status_bytes = ((tiles + 1) * 4 + 255) / 256 * 256;
+  const size_t agg_bytes = (tiles * csz + 255) / 256 * 256;
+  if (int st = ensure_workspace(p, status_bytes + 2 * agg_bytes)) return st;
+  void* status = p->ws.ptr;
+  void* agg = (char*)p->ws.ptr + status_bytes;
+  void* incl = (char*)p->ws.ptr + status_bytes + agg_bytes;
+  SCL_CUDA(cudaMemsetAsync(status, 0, (tiles + 1) * 4, rt().stream));
+  unsigned int flags = sh->flags & (SCL_SHAPE_INCLUSIVE | SCL_SHAPE_REVERSE);
+  int aligned = (aligned16(in) && aligned16(out)) ? 1 : 0;
+  unsigned int spin = spin_of(tu);
+  unsigned int* err = rt().dev_err;
+  ArgPack pack;
+  pack.ptrs = {&in, &out, &n, &flags, &aligned, &status, &agg, &incl, &spin, &err};
+  if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
+    return st;
+  p->last_variant = SCL_VARIANT_VECTOR;
+  return launch(fn, dim3((unsigned)tiles), dim3(256), 0, pack);
+}
+
+// ---- MapOverlap -----------------------------------------------------------------
+extern "C" int scl_launch_mapoverlap(scl_program* p, const scl_shape* sh, void* const* bufs,
+                                     const void* extra, size_t extra_bytes, const scl_tuning* tu) {
+  if (int st = check_prog(p, {SCL_KIND_MAPOVERLAP})) return st;
+  if (!sh || !bufs || !bufs[0] || !bufs[1]) return fail(SCL_ERR_ARG, "mapoverlap needs {in, out}");
+  void* in = bufs[0];
+  void* out = bufs[1];
+  uint64_t rows = sh->rows, cols = sh->cols;
+  if (rows == 0 || cols == 0) return SCL_OK;
+  if (rows > 0x7fffffffull || cols > 0x7fffffffull) return fail(SCL_ERR_ARG, "matrix too large");
+  const size_t tsz = p->type_sizes[0];
+  const int R = p->overlap_range, PY = 4, TW = 32, TH = 8 * PY;
+  const int xal = tsz <= 16 ? (int)std::max<size_t>(1, 16 / tsz) : 1;
+  const int xlead = (R + xal - 1) / xal * xal;
+  const int win_w = (xlead + TW + R + xal - 1) / xal * xal;
+  const int win_h = TH + 2 * R;
+  const size_t win_bytes = (size_t)win_w * win_h * tsz;
+  if (win_bytes > rt().smem_optin) return fail(SCL_ERR_ARG, "overlap range too large for shared memory");
+  dim3 grid((unsigned)((cols + TW - 1) / TW), (unsigned)((rows + TH - 1) / TH)), block(32, 8);
+  if (grid.y > 65535) return fail(SCL_ERR_ARG, "matrix has too many rows for one launch");
+  const bool want_tma = !(tu && tu->variant == SCL_VARIANT_LDST);
+  const bool tma_ok = (tsz == 1 || tsz == 2 || tsz == 4 || tsz == 8) && (cols * tsz) % 16 == 0 &&
+                      aligned16(in) && win_w <= 256 && win_h <= 256;
+  unsigned int spin = spin_of(tu);
+  unsigned int* err = rt().dev_err;
+  if (want_tma && tma_ok) {
+    CUfunction fn = find_kernel(p, "scl_mapoverlap_tma");
+    if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_mapoverlap_tma missing");
+    alignas(64) CUtensorMap tmap;
+    CUtensorMapDataType dt = tsz == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                           : tsz == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16
+                           : tsz == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32
+                                      : CU_TENSOR_MAP_DATA_TYPE_UINT64;
+    cuuint64_t dims[2] = {cols, rows};
+    cuuint64_t strides[1] = {cols * tsz};
+    cuuint32_t box[2] = {(cuuint32_t)win_w, (cuuint32_t)win_h};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = rt().drv.cuTensorMapEncodeTiled(
+        &tmap, dt, 2, in, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cu_fail(r, "cuTensorMapEncodeTiled");
+    ArgPack pack;
+    pack.ptrs = {&tmap, &out, &rows, &cols, &spin, &err};
+    if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
+      return st;
+    p->last_variant = SCL_VARIANT_TMA;
+    return launch(fn, grid, block, win_bytes, pack);
+  }
+  CUfunction fn = find_kernel(p, "scl_mapoverlap_ldst");
+  if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_mapoverlap_ldst missing");
+  ArgPack pack;
+  pack.ptrs = {&in, &out, &rows, &cols};
+  if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
+    return st;
+  p->last_variant = SCL_VARIANT_LDST;
+  return launch(fn, grid, block, win_bytes, pack);
+}
+
+// ---- AllPairs -------------------------------------------------------------------
+extern "C" int scl_launch_allpairs(scl_program* p, const scl_shape* sh, void* const* bufs,
+                                   const void* extra, size_t extra_bytes, const scl_tuning* tu) {
+  if (int st = check_prog(p, {SCL_KIND_ALLPAIRS, SCL_KIND_ALLPAIRS_GENERIC})) return st;
+  if (!sh || !bufs || !bufs[0] || !bufs[1] || !bufs[2])
+    return fail(SCL_ERR_ARG, "allpairs needs {left, right, out}");
+  void* A = bufs[0];
+  void* B = bufs[1];
+  void* P = bufs[2];
+  if (sh->rows > 0xffffffffull || sh->cols > 0xffffffffull || sh->dim > 0xffffffffull)
+    return fail(SCL_ERR_ARG, "AllPairs dimensions must fit 32 bits");
+  unsigned int M = (unsigned int)sh->rows, N = (unsigned int)sh->cols, K = (unsigned int)sh->dim;
+  if (M == 0 || N == 0) return SCL_OK;
+  if (K == 0) return fail(SCL_ERR_ARG, "AllPairs inner dimension is 0");
+  if (p->kind == SCL_KIND_ALLPAIRS) {
+    const uint32_t want = tu ? tu->variant : SCL_VARIANT_AUTO;
+    if (p->tc_eligible && want != SCL_VARIANT_SIMT && extra_bytes == 0 &&
+        allpairs_tc_supported(M, N, K, A, B, P)) {
+      p->last_variant = SCL_VARIANT_TC3XBF16;
+      return allpairs_tc_launch((const float*)A, (const float*)B, (float*)P, M, N, K, rt().stream,
+                                spin_of(tu), rt().dev_err);
+    }
+    if (want == SCL_VARIANT_TC3XBF16)
+      return fail(SCL_ERR_UNSUPPORTED, "the tensor-core AllPairs needs zip x*y, reduce x+y, identity 0, "
+                                       "float operands, no extra arguments and supported shapes");
+    CUfunction fn = find_kernel(p, "scl_allpairs_simt");
+    if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_allpairs_simt missing");
+    int vec_a = (p->type_sizes[0] == 4 && K % 4 == 0 && aligned16(A)) ? 1 : 0;
+    int vec_b = (p->type_sizes[1] == 4 && N % 4 == 0 && aligned16(B)) ? 1 : 0;
+    ArgPack pack;
+    pack.ptrs = {&A, &B, &P, &M, &N, &K, &vec_a, &vec_b};
+    if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
+      return st;
+    dim3 grid((N + 127) / 128, (M + 127) / 128);
+    if (grid.y > 65535) return fail(SCL_ERR_ARG, "too many rows");
+    p->last_variant = SCL_VARIANT_SIMT;
+    return launch(fn, grid, dim3(256), 0, pack);
+  }
+  CUfunction fn = find_kernel(p, "scl_allpairs_generic");
+  if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_allpairs_generic missing");
+  const size_t s0 = p->type_sizes[0], s1 = p->type_sizes[1];
+  size_t stage = ((16ull * K * s0 + 15) & ~15ull) + 16ull * K * s1;
+  int staged = (stage + 1024 <= rt().smem_optin) ? 1 : 0;
+  ArgPack pack;
+  pack.ptrs = {&A, &B, &P, &K, &M, &N, &staged};
+  if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
+    return st;
+  dim3 grid((N + 15) / 16, (M + 15) / 16);
+  if (grid.y > 65535) return fail(SCL_ERR_ARG, "too many rows");
+  p->last_variant = SCL_VARIANT_SIMT;
+  return launch(fn, grid, dim3(16, 16), staged ? stage : 0, pack);
+}
+

@@ -1,0 +1,603 @@
+// Program assembly and JIT compilation: the GB300 counterpart of
+// detail::Program (src/Program.cpp:83-250) and the per-skeleton
+// createAndBuildProgram() bodies (MapDef.h:170-212, ZipDef.h:177-224,
+// ReduceDef.h:248-275, ScanDef.h:263-297, MapOverlapDef.h:181-248,
+// AllPairsDef.h:213-344).
+//
+// The generated CUDA source is, in order:
+//   prelude (OpenCL C vocabulary)          -- templates/prelude.cuh
+//   SCL_TYPE_n typedefs, skeleton defines
+//   definitions the user function sees    -- Index, IndexPoint, input_matrix_t,
+//                                             lmatrix_t / rmatrix_t
+//   common definitions (SKELCL_COMMON_DEFINITION, src/Source.cpp:118-126)
+//   user source with the function renamed (stooling renameFunction)
+//   extra-parameter plumbing macros (stooling transferParameters /
+//                                    transferArguments / fixKernelParameter)
+//   skeleton template                      -- templates/<skeleton>.cuh
+// and is compiled by NVRTC for sm_103a into a cubin, loaded as a module.
+// The cache key is the SHA-1 of the generated source + options, as the
+// reference keys its binary cache by util::hash of the source
+// (src/Program.cpp:62-75,136-175,252-281).  Environment switches kept from the
+// reference: SKELCL_LOAD_BINARY=YES, SKELCL_SAVE_BINARY=YES,
+// SKELCL_PRINT_BUILD_LOG=YES; SKELCL_CACHE_DIR picks the cache directory.
+#include <nvrtc.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <sys/stat.h>
+
+#include "internal.h"
+
+// Template sources, embedded at build time (generated file).
+extern const char* scl_tpl_prelude;
+extern const char* scl_tpl_elementwise;
+extern const char* scl_tpl_reduce;
+extern const char* scl_tpl_scan;
+extern const char* scl_tpl_mapoverlap_pre;
+extern const char* scl_tpl_mapoverlap;
+extern const char* scl_tpl_allpairs_pre;
+extern const char* scl_tpl_allpairs;
+
+namespace scl {
+namespace {
+
+std::string env(const char* name) {
+  const char* v = std::getenv(name);
+  return v ? std::string(v) : std::string();
+}
+
+bool env_yes(const char* name) {
+  std::string v = env(name);
+  return v == "YES" || v == "yes" || v == "1" || v == "ON" || v == "on";
+}
+
+std::string strip_opencl_pragmas(const std::string& s) {
+  std::istringstream in(s);
+  std::string line, out;
+  while (std::getline(in, line)) {
+    size_t p = line.find_first_not_of(" \t");
+    if (p != std::string::npos && line.compare(p, 7, "#pragma") == 0 &&
+        line.find("OPENCL") != std::string::npos)
+      continue;
+    out += line;
+    out += '\n';
+  }
+  return out;
+}
+
+// Number of leading parameters the skeleton itself supplies.
+int skeleton_arity(int kind) {
+  switch (kind) {
+    case SCL_KIND_ZIP:
+    case SCL_KIND_ZIP_VOID:
+    case SCL_KIND_REDUCE:
+    case SCL_KIND_SCAN:
+      return 2;
+    case SCL_KIND_ALLPAIRS_GENERIC:
+      return 3;
+    case SCL_KIND_ALLPAIRS:
+      return 2;  // both the Reduce and the Zip take two
+    default:
+      return 1;
+  }
+}
+
+struct ExtraMacros {
+  std::string params, user, setup, args;
+};
+
+void append_extra(const std::vector<Param>& ps, size_t first_index, ExtraMacros* m,
+                  std::string* args_only) {
+  for (size_t i = 0; i < ps.size(); ++i) {
+    const Param& p = ps[i];
+    std::string nm = "scl_x" + std::to_string(first_index + i);
+    switch (p.kind) {
+      case ParamKind::Value:
+      case ParamKind::Buffer:
+        m->params += ", " + p.type + " " + nm;
+        m->user += ", " + p.type + " " + nm;
+        break;
+      case ParamKind::Matrix:
+        m->params += ", " + p.elem + "* " + nm + "_d, unsigned int " + nm + "_c";
+        m->setup += p.elem + "_matrix_t " + nm + "; " + nm + ".data = " + nm + "_d; " + nm +
+                    ".col_count = " + nm + "_c; ";
+        m->user += ", " + p.elem + "_matrix_t " + nm;
+        break;
+      case ParamKind::Local:
+        m->params += ", unsigned int " + nm + "_o";
+        m->setup += p.type + " " + nm + " = (" + p.type + ")(scl_dyn_smem + " + nm + "_o); ";
+        m->user += ", " + p.type + " " + nm;
+        break;
+    }
+    m->args += ", " + nm;
+    if (args_only) *args_only += ", " + nm;
+  }
+}
+
+bool neutral_is_zero(const std::string& s) {
+  if (s.empty()) return true;
+  char* end = nullptr;
+  double v = std::strtod(s.c_str(), &end);
+  while (end && *end && (std::isspace((unsigned char)*end) || *end == 'f' || *end == 'F' ||
+                         *end == 'u' || *end == 'U' || *end == 'l' || *end == 'L'))
+    ++end;
+  return end && *end == '\0' && v == 0.0;
+}
+
+struct Assembly {
+  std::string source;
+  std::vector<std::string> kernels;  // name expressions
+};
+
+int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly* out,
+             std::string* err) {
+  const int kind = d->kind;
+  const std::string func = d->func ? d->func : "func";
+  const std::string src = strip_opencl_pragmas(d->source ? d->source : "");
+  if (src.find_first_not_of(" \t\r\n") == std::string::npos) {
+    *err = "empty user source";
+    return SCL_ERR_ARG;
+  }
+  std::ostringstream s;
+  s << "// generated by libskelcl_cuda\n#define SCL_KIND " << kind << "\n";
+  const bool point = kind == SCL_KIND_MAP_POINT || kind == SCL_KIND_MAP_POINT_VOID;
+  if (point) s << "#define SCL_WI_SWAP 1\n#define SCL_WORK_DIM 2\n";
+  if (kind == SCL_KIND_MAPOVERLAP) s << "#define SCL_WORK_DIM 2\n";
+  s << scl_tpl_prelude << "\n";
+  for (int i = 0; i < d->n_types; ++i)
+    s << "typedef " << d->type_names[i] << " SCL_TYPE_" << i << ";\n";
+  if (kind == SCL_KIND_MAP_INDEX || kind == SCL_KIND_MAP_INDEX_VOID)
+    s << "typedef size_t Index;\n";
+  if (point) s << "typedef struct { size_t x; size_t y; } IndexPoint;\n";
+  if (kind == SCL_KIND_REDUCE || kind == SCL_KIND_SCAN || kind == SCL_KIND_ALLPAIRS)
+    s << "#define SCL_IDENTITY (" << (d->identity && *d->identity ? d->identity : "0") << ")\n";
+  if (kind == SCL_KIND_MAPOVERLAP) {
+    std::string neutral = d->neutral && *d->neutral ? d->neutral : "0";
+    s << "#define SCL_OVERLAP_RANGE " << d->overlap_range << "\n"
+      << "#define SCL_PADDING " << (d->padding == SCL_PAD_NEAREST ? 1 : 0) << "\n"
+      << "#define SCL_NEUTRAL (" << neutral << ")\n"
+      << "#define SCL_NEUTRAL_IS_ZERO " << (neutral_is_zero(neutral) ? 1 : 0) << "\n"
+      << "#define SCL_PY 4\n"
+      << scl_tpl_mapoverlap_pre << "\n";
+  }
+  if (kind == SCL_KIND_ALLPAIRS_GENERIC) s << scl_tpl_allpairs_pre << "\n";
+  if (d->common_source && *d->common_source)
+    s << "// ---- common definitions\n" << strip_opencl_pragmas(d->common_source) << "\n";
+
+  ExtraMacros em;
+  p->extra.clear();
+  p->n_reduce_extra = 0;
+  std::string zip_args, reduce_args;
+  if (kind == SCL_KIND_ALLPAIRS) {
+    const std::string func2 = d->func2 ? d->func2 : "func";
+    const std::string src2 = strip_opencl_pragmas(d->source2 ? d->source2 : "");
+    FuncSig rs, zs;
+    if (!parse_function(src, func, &rs, err)) { *err = "Reduce source: " + *err; return SCL_ERR_COMPILE; }
+    if (!parse_function(src2, func2, &zs, err)) { *err = "Zip source: " + *err; return SCL_ERR_COMPILE; }
+    if (rs.params.size() < 2 || zs.params.size() < 2) {
+      *err = "AllPairs: the Reduce and Zip functions need two parameters each";
+      return SCL_ERR_COMPILE;
+    }
+    std::vector<Param> rx(rs.params.begin() + 2, rs.params.end());
+    std::vector<Param> zx(zs.params.begin() + 2, zs.params.end());
+    s << "// ---- reduce user source\n" << rename_identifier(src, func, "USR_REDUCE") << "\n";
+    s << "// ---- zip user source\n" << rename_identifier(src2, func2, "USR_ZIP") << "\n";
+    append_extra(rx, 0, &em, &reduce_args);
+    append_extra(zx, rx.size(), &em, &zip_args);
+    p->extra = rx;
+    p->extra.insert(p->extra.end(), zx.begin(), zx.end());
+    p->n_reduce_extra = rx.size();
+    p->uses_workitem = false;
+    // tensor-core eligibility: zip x*y, reduce x+y, identity 0, all float, no extras
+    auto body_is = [](const std::string& text, const FuncSig& sg, const char* op) {
+      std::string body = text.substr(sg.def_begin, sg.def_end - sg.def_begin);
+      size_t b = body.find('{');
+      std::string inner;
+      for (char c : body.substr(b)) if (!std::isspace((unsigned char)c)) inner += c;
+      const std::string a = sg.params[0].name, bb = sg.params[1].name;
+      return inner == std::string("{return") + a + op + bb + ";}" ||
+             inner == std::string("{return") + bb + op + a + ";}" ||
+             inner == std::string("{return(") + a + op + bb + ");}";
+    };
+    std::string id = d->identity && *d->identity ? d->identity : "0";
+    bool all_float = d->n_types == 3;
+    for (int i = 0; i < d->n_types && all_float; ++i) all_float = std::string(d->type_names[i]) == "float";
+    p->tc_eligible = all_float && rx.empty() && zx.empty() && neutral_is_zero(id) &&
+                     body_is(src, rs, "+") && body_is(src2, zs, "*");
+  } else {
+    FuncSig sig;
+    if (!parse_function(src, func, &sig, err)) return SCL_ERR_COMPILE;
+    const int k = skeleton_arity(kind);
+    if ((int)sig.params.size() < k) {
+      *err = "function '" + func + "' takes " + std::to_string(sig.params.size()) +
+             " parameters; the skeleton passes " + std::to_string(k);
+      return SCL_ERR_COMPILE;
+    }
+    std::vector<Param> ex(sig.params.begin() + k, sig.params.end());
+    const char* target = (kind == SCL_KIND_MAPOVERLAP || kind == SCL_KIND_ALLPAIRS_GENERIC)
+                             ? "USR_FUNC" : "SCL_FUNC";
+    std::string renamed = rename_identifier(src, func, target);
+    s << "// ---- user source\n" << renamed << "\n";
+    p->uses_workitem = source_uses_workitem(src);
+    if (want_f64) {
+      // FP64 twin of the user function for cross-block carries
+      FuncSig rsig;
+      std::string e2;
+      if (parse_function(renamed, target, &rsig, &e2)) {
+        std::string def = renamed.substr(rsig.def_begin, rsig.def_end - rsig.def_begin);
+        def = rename_identifier(def, "float", "double");
+        def = rename_identifier(def, target, "SCL_FUNC_C");
+        s << "// ---- FP64 twin for carries\n" << def << "\n";
+      }
+    }
+    append_extra(ex, 0, &em, nullptr);
+    p->extra = ex;
+  }
+  s << "#define SCL_EXTRA_PARAMS " << em.params << "\n"
+    << "#define SCL_USER_PARAMS " << em.user << "\n"
+    << "#define SCL_EXTRA_SETUP " << em.setup << "\n"
+    << "#define SCL_EXTRA_ARGS " << em.args << "\n"
+    << "#define SCL_REDUCE_ARGS " << reduce_args << "\n"
+    << "#define SCL_ZIP_ARGS " << zip_args << "\n";
+  if (kind == SCL_KIND_REDUCE || kind == SCL_KIND_SCAN) {
+    if (want_f64) s << "typedef double SCL_CARRY_T;\n";
+    else s << "typedef SCL_TYPE_0 SCL_CARRY_T;\n#define SCL_FUNC_C SCL_FUNC\n";
+  }
+  s << "// ---- skeleton template\n";
+  switch (kind) {
+    case SCL_KIND_MAP: case SCL_KIND_MAP_VOID: case SCL_KIND_MAP_INDEX:
+    case SCL_KIND_MAP_INDEX_VOID: case SCL_KIND_MAP_POINT: case SCL_KIND_MAP_POINT_VOID:
+    case SCL_KIND_ZIP: case SCL_KIND_ZIP_VOID:
+      s << scl_tpl_elementwise;
+      out->kernels = {"scl_map_k<1>", "scl_map_k<2>", "scl_map_k<4>", "scl_map_simple"};
+      break;
+    case SCL_KIND_REDUCE:
+      s << scl_tpl_reduce;
+      out->kernels = {"scl_reduce_k<1>", "scl_reduce_k<2>", "scl_reduce_k<4>"};
+      break;
+    case SCL_KIND_SCAN:
+      s << scl_tpl_reduce << "\n" << scl_tpl_scan;
+      out->kernels = {"scl_scan_k<2>", "scl_scan_k<4>"};
+      break;
+    case SCL_KIND_MAPOVERLAP:
+      s << scl_tpl_mapoverlap;
+      out->kernels = {"scl_mapoverlap_ldst", "scl_mapoverlap_tma"};
+      break;
+    case SCL_KIND_ALLPAIRS:
+      s << scl_tpl_allpairs;
+      out->kernels = {"scl_allpairs_simt"};
+      break;
+    case SCL_KIND_ALLPAIRS_GENERIC:
+      s << scl_tpl_allpairs;
+      out->kernels = {"scl_allpairs_generic"};
+      break;
+    default:
+      *err = "unknown skeleton kind " + std::to_string(kind);
+      return SCL_ERR_ARG;
+  }
+  // element / carry sizes, read back by the host after the module loads
+  s << "\nextern \"C\" __device__ const unsigned int scl_type_sizes[4] = {";
+  for (int i = 0; i < 3; ++i)
+    s << (i < d->n_types ? "(unsigned int)sizeof(SCL_TYPE_" + std::to_string(i) + ")" : std::string("0u")) << ", ";
+  s << ((kind == SCL_KIND_REDUCE || kind == SCL_KIND_SCAN) ? "(unsigned int)sizeof(SCL_CARRY_T)" : "0u")
+    << "};\n";
+  out->source = s.str();
+  return SCL_OK;
+}
+
+const char* kNvrtcOpts[] = {"-arch=sm_103a", "-std=c++17", "-default-device",
+                            "-diag-suppress=177,550,174,1835", "-lineinfo"};
+const int kNvrtcOptCount = 5;
+
+std::mutex g_cache_mu;
+std::map<std::string, std::pair<std::string, std::map<std::string, std::string>>> g_mem_cache;
+
+std::string cache_dir() {
+  std::string d = env("SKELCL_CACHE_DIR");
+  if (!d.empty()) return d;
+  std::string home = env("HOME");
+  return (home.empty() ? std::string("/tmp") : home) + "/.cache/skelcl_gb300";
+}
+
+// Serialised cache entry: "SCLBIN1\n" n_names \n (expr \n lowered \n)* cubin
+bool load_disk(const std::string& key, std::string* cubin,
+               std::map<std::string, std::string>* names) {
+  std::ifstream f(cache_dir() + "/" + key + ".sm_103a.skelcl", std::ios::binary);
+  if (!f) return false;
+  std::string magic;
+  std::getline(f, magic);
+  if (magic != "SCLBIN1") return false;
+  std::string line;
+  std::getline(f, line);
+  int n = std::atoi(line.c_str());
+  for (int i = 0; i < n; ++i) {
+    std::string a, b;
+    std::getline(f, a);
+    std::getline(f, b);
+    (*names)[a] = b;
+  }
+  std::ostringstream rest;
+  rest << f.rdbuf();
+  *cubin = rest.str();
+  return !cubin->empty();
+}
+
+void save_disk(const std::string& key, const std::string& cubin,
+               const std::map<std::string, std::string>& names) {
+  std::string dir = cache_dir();
+  std::string acc;
+  for (size_t i = 0; i <= dir.size(); ++i) {
+    if (i == dir.size() || dir[i] == '/') {
+      if (!acc.empty()) mkdir(acc.c_str(), 0755);
+    }
+    if (i < dir.size()) acc += dir[i];
+  }
+  std::string tmp = dir + "/" + key + ".tmp";
+  {
+    std::ofstream f(tmp, std::ios::binary);
+    if (!f) return;
+    f << "SCLBIN1\n" << names.size() << "\n";
+    for (auto& kv : names) f << kv.first << "\n" << kv.second << "\n";
+    f.write(cubin.data(), (std::streamsize)cubin.size());
+  }
+  std::rename(tmp.c_str(), (dir + "/" + key + ".sm_103a.skelcl").c_str());
+}
+
+int nvrtc_compile(const Assembly& a, std::string* cubin,
+                  std::map<std::string, std::string>* lowered, std::string* log) {
+  nvrtcProgram prog;
+  nvrtcResult r = nvrtcCreateProgram(&prog, a.source.c_str(), "skelcl_program.cu", 0, nullptr, nullptr);
+  if (r != NVRTC_SUCCESS) {
+    *log = std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r);
+    return SCL_ERR_COMPILE;
+  }
+  for (auto& k : a.kernels)
+    if (k.find('<') != std::string::npos) nvrtcAddNameExpression(prog, k.c_str());
+  r = nvrtcCompileProgram(prog, kNvrtcOptCount, kNvrtcOpts);
+  size_t ls = 0;
+  nvrtcGetProgramLogSize(prog, &ls);
+  std::string lg(ls, '\0');
+  if (ls) nvrtcGetProgramLog(prog, &lg[0]);
+  while (!lg.empty() && lg.back() == '\0') lg.pop_back();
+  *log = lg;
+  if (r != NVRTC_SUCCESS) {
+    nvrtcDestroyProgram(&prog);
+    return SCL_ERR_COMPILE;
+  }
+  size_t n = 0;
+  nvrtcGetCUBINSize(prog, &n);
+  cubin->assign(n, '\0');
+  nvrtcGetCUBIN(prog, &(*cubin)[0]);
+  for (auto& k : a.kernels) {
+    if (k.find('<') != std::string::npos) {
+      const char* low = nullptr;
+      if (nvrtcGetLoweredName(prog, k.c_str(), &low) == NVRTC_SUCCESS && low) (*lowered)[k] = low;
+    } else {
+      (*lowered)[k] = k;
+    }
+  }
+  nvrtcDestroyProgram(&prog);
+  return SCL_OK;
+}
+
+void copy_log(const std::string& s, char* log, size_t cap) {
+  if (!log || cap == 0) return;
+  size_t n = s.size() < cap - 1 ? s.size() : cap - 1;
+  std::memcpy(log, s.data(), n);
+  log[n] = '\0';
+}
+
+}  // namespace
+
+CUfunction find_kernel(scl_program* p, const std::string& name) {
+  auto it = p->kernels.find(name);
+  return it == p->kernels.end() ? nullptr : it->second.fn;
+}
+
+int ensure_workspace(scl_program* p, size_t bytes) {
+  if (p->ws.bytes >= bytes) return SCL_OK;
+  if (p->ws.ptr) {
+    cudaStreamSynchronize(rt().stream);
+    cudaFree(p->ws.ptr);
+    p->ws.ptr = nullptr;
+    p->ws.bytes = 0;
+  }
+  size_t sz = bytes < 4096 ? 4096 : bytes;
+  cudaError_t e = cudaMalloc(&p->ws.ptr, sz);
+  if (e != cudaSuccess) return fail(SCL_ERR_OOM, "workspace allocation of " + std::to_string(sz) + " bytes failed");
+  // zeroed once: reduce tickets rely on it and reset themselves afterwards
+  e = cudaMemset(p->ws.ptr, 0, sz);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(workspace)");
+  p->ws.bytes = sz;
+  return SCL_OK;
+}
+
+}  // namespace scl
+
+using namespace scl;
+
+extern "C" int scl_sha1_hex(const void* data, size_t bytes, char* out41) {
+  if (!out41 || (!data && bytes)) return fail(SCL_ERR_ARG, "scl_sha1_hex: null pointer");
+  std::string h = sha1_hex(data, bytes);
+  std::memcpy(out41, h.c_str(), 41);
+  return SCL_OK;
+}
+
+extern "C" int scl_program_source(const scl_program_desc* desc, char* out, size_t cap,
+                                  size_t* needed) {
+  if (!desc) return fail(SCL_ERR_ARG, "scl_program_source: null desc");
+  scl_program tmp;
+  tmp.kind = desc->kind;
+  Assembly a;
+  std::string err;
+  bool f64 = (desc->kind == SCL_KIND_REDUCE || desc->kind == SCL_KIND_SCAN) &&
+             desc->n_types >= 1 && desc->type_names[0] &&
+             std::string(desc->type_names[0]) == "float" &&
+             !(desc->flags & SCL_PROG_NO_F64_CARRY);
+  int st = assemble(desc, &tmp, f64, &a, &err);
+  if (st != SCL_OK) return fail(st, err);
+  if (needed) *needed = a.source.size() + 1;
+  if (out && cap) copy_log(a.source, out, cap);
+  return SCL_OK;
+}
+
+extern "C" int scl_program_build(const scl_program_desc* desc, scl_program** out, char* log,
+                                 size_t log_cap) {
+  if (!desc || !out) return fail(SCL_ERR_ARG, "scl_program_build: null argument");
+  *out = nullptr;
+  if (desc->n_types < 0 || desc->n_types > 3) return fail(SCL_ERR_ARG, "n_types out of range");
+  for (int i = 0; i < desc->n_types; ++i)
+    if (!desc->type_names[i] || !*desc->type_names[i])
+      return fail(SCL_ERR_ARG, "missing type name " + std::to_string(i));
+  if (desc->kind == SCL_KIND_MAPOVERLAP && (desc->overlap_range < 0 || desc->overlap_range > 64))
+    return fail(SCL_ERR_ARG, "overlap range must be in [0, 64]");
+  std::unique_ptr<scl_program> p(new scl_program);
+  p->kind = desc->kind;
+  p->overlap_range = desc->overlap_range;
+  p->padding = desc->padding;
+  for (int i = 0; i < desc->n_types; ++i) p->type_names.push_back(desc->type_names[i]);
+
+  bool want_f64 = (desc->kind == SCL_KIND_REDUCE || desc->kind == SCL_KIND_SCAN) &&
+                  desc->n_types >= 1 && std::string(desc->type_names[0]) == "float" &&
+                  !(desc->flags & SCL_PROG_NO_F64_CARRY);
+  std::string cubin, nvlog, err;
+  std::map<std::string, std::string> lowered;
+  Assembly a;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    bool f64 = want_f64 && attempt == 0;
+    int st = assemble(desc, p.get(), f64, &a, &err);
+    if (st != SCL_OK) {
+      copy_log(err, log, log_cap);
+      return fail(st, err);
+    }
+    std::string key;
+    {
+      std::string k = a.source;
+      for (int i = 0; i < kNvrtcOptCount; ++i) k += std::string("\n") + kNvrtcOpts[i];
+      key = sha1_hex(k.data(), k.size());
+    }
+    p->hash = key;
+    bool have = false;
+    {
+      std::lock_guard<std::mutex> g(g_cache_mu);
+      auto it = g_mem_cache.find(key);
+      if (it != g_mem_cache.end()) {
+        cubin = it->second.first;
+        lowered = it->second.second;
+        have = true;
+      }
+    }
+    if (!have && env_yes("SKELCL_LOAD_BINARY")) have = load_disk(key, &cubin, &lowered);
+    if (!have) {
+      lowered.clear();
+      st = nvrtc_compile(a, &cubin, &lowered, &nvlog);
+      if (env_yes("SKELCL_PRINT_BUILD_LOG") && !nvlog.empty())
+        std::fprintf(stderr, "[skelcl] NVRTC build log:\n%s\n", nvlog.c_str());
+      if (st != SCL_OK) {
+        if (f64) continue;  // retry with carries in the element type
+        std::string msg = "NVRTC compilation failed:\n" + nvlog;
+        copy_log(msg, log, log_cap);
+        return fail(SCL_ERR_COMPILE, msg);
+      }
+      std::lock_guard<std::mutex> g(g_cache_mu);
+      g_mem_cache[key] = {cubin, lowered};
+      if (env_yes("SKELCL_SAVE_BINARY")) save_disk(key, cubin, lowered);
+    }
+    p->f64_carry = f64;
+    break;
+  }
+  p->source = a.source;
+  if (int st = require_init()) {
+    copy_log("scl_init() has not been called", log, log_cap);
+    return st;
+  }
+  Driver& drv = rt().drv;
+  CUresult r = drv.cuModuleLoadData(&p->module, cubin.data());
+  if (r != CUDA_SUCCESS) {
+    std::string msg = "cuModuleLoadData failed";
+    copy_log(msg, log, log_cap);
+    return cu_fail(r, "cuModuleLoadData");
+  }
+  for (auto& kv : lowered) {
+    CUfunction fn = nullptr;
+    r = drv.cuModuleGetFunction(&fn, p->module, kv.second.c_str());
+    if (r != CUDA_SUCCESS) return cu_fail(r, ("cuModuleGetFunction " + kv.first).c_str());
+    p->kernels[kv.first] = Kernel{fn, kv.second};
+  }
+  {
+    CUdeviceptr gp = 0;
+    size_t gsz = 0;
+    r = drv.cuModuleGetGlobal(&gp, &gsz, p->module, "scl_type_sizes");
+    if (r != CUDA_SUCCESS) return cu_fail(r, "cuModuleGetGlobal(scl_type_sizes)");
+    unsigned int sz[4] = {0, 0, 0, 0};
+    cudaError_t e = cudaMemcpy(sz, (const void*)gp, sizeof(sz), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(scl_type_sizes)");
+    for (int i = 0; i < desc->n_types; ++i) p->type_sizes.push_back(sz[i]);
+    p->carry_size = sz[3];
+  }
+  if (log && log_cap) copy_log(nvlog, log, log_cap);
+  *out = p.release();
+  return SCL_OK;
+}
+
+extern "C" int scl_program_compile(const scl_program_desc* desc, char* log, size_t log_cap) {
+  if (!desc) return fail(SCL_ERR_ARG, "scl_program_compile: null desc");
+  scl_program tmp;
+  tmp.kind = desc->kind;
+  bool want_f64 = (desc->kind == SCL_KIND_REDUCE || desc->kind == SCL_KIND_SCAN) &&
+                  desc->n_types >= 1 && desc->type_names[0] &&
+                  std::string(desc->type_names[0]) == "float" &&
+                  !(desc->flags & SCL_PROG_NO_F64_CARRY);
+  std::string err, nvlog, cubin;
+  std::map<std::string, std::string> lowered;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    Assembly a;
+    bool f64 = want_f64 && attempt == 0;
+    int st = assemble(desc, &tmp, f64, &a, &err);
+    if (st != SCL_OK) {
+      copy_log(err, log, log_cap);
+      return fail(st, err);
+    }
+    st = nvrtc_compile(a, &cubin, &lowered, &nvlog);
+    if (st == SCL_OK) {
+      copy_log(nvlog, log, log_cap);
+      return SCL_OK;
+    }
+    if (!f64) break;
+  }
+  std::string msg = "NVRTC compilation failed:\n" + nvlog;
+  copy_log(msg, log, log_cap);
+  return fail(SCL_ERR_COMPILE, msg);
+}
+
+extern "C" int scl_program_release(scl_program* p) {
+  if (!p) return SCL_OK;
+  if (rt().initialized) {
+    cudaStreamSynchronize(rt().stream);
+    if (p->ws.ptr) cudaFree(p->ws.ptr);
+    if (p->module) rt().drv.cuModuleUnload(p->module);
+  }
+  delete p;
+  return SCL_OK;
+}
+
+extern "C" int scl_program_extra_count(const scl_program* p, int* count) {
+  if (!p || !count) return fail(SCL_ERR_ARG, "null argument");
+  *count = (int)p->extra.size();
+  return SCL_OK;
+}
+
+extern "C" int scl_program_hash(const scl_program* p, char* out41) {
+  if (!p || !out41) return fail(SCL_ERR_ARG, "null argument");
+  std::memcpy(out41, p->hash.c_str(), 41);
+  return SCL_OK;
+}
+
+extern "C" int scl_program_last_variant(const scl_program* p, uint32_t* variant) {
+  if (!p || !variant) return fail(SCL_ERR_ARG, "null argument");
+  *variant = p->last_variant;
+  return SCL_OK;
+}

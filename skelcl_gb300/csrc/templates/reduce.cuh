@@ -1,0 +1,196 @@
+// ---------------------------------------------------------------------------
+// Reduce for sm_103a: ONE launch.  Replaces the reference's two kernels
+// SCL_REDUCE_1 (8192 work-items, strided fold) and SCL_REDUCE_2 (one work-group
+// tree) of include/SkelCL/detail/ReduceKernel.cl:51-128 and
+// include/SkelCL/detail/ReduceDef.h:98-245.
+//
+// Semantics kept from the reference:
+//  * the identity is not used to seed the fold: every partial starts from a
+//    real element (ReduceKernel.cl:60-61), so a non-neutral `id` string has
+//    no effect, as in the reference;
+//  * the operator is assumed associative and commutative (the reference folds
+//    element j, j+8192, j+2*8192 ... and then a tree);
+//  * the result is a one-element vector (ReduceDef.h:113-121).
+// Empty input (the reference reads out of bounds there) yields SCL_IDENTITY.
+//
+// Shape: grid-stride 16-byte loads, per-thread fold in T, then warp-shuffle
+// and block folds in the carry type SCL_CARRY_T (double for float element
+// types: "cross-block carries in FP64"), one partial per block, and the last
+// block to finish (atomic ticket) folds the partials in block order and
+// resets the ticket for the next launch.
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ T scl_shfl_down(const T& v, int off) {
+  constexpr int W = (int)((sizeof(T) + 3) / 4);
+  unsigned int w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int i = 0; i < W; ++i) w[i] = __shfl_down_sync(0xffffffffu, w[i], off);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ T scl_shfl_up(const T& v, int off) {
+  constexpr int W = (int)((sizeof(T) + 3) / 4);
+  unsigned int w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int i = 0; i < W; ++i) w[i] = __shfl_up_sync(0xffffffffu, w[i], off);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ T scl_shfl_idx(const T& v, int src) {
+  constexpr int W = (int)((sizeof(T) + 3) / 4);
+  unsigned int w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int i = 0; i < W; ++i) w[i] = __shfl_sync(0xffffffffu, w[i], src);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+// Coherent (L1-bypassing) copy of a value written by another block.
+template <typename T>
+__device__ __forceinline__ T scl_ld_cg(const T* p) {
+  T r;
+  if constexpr (sizeof(T) % 4 == 0) {
+    unsigned int w[sizeof(T) / 4];
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(T) / 4); ++i)
+      w[i] = *((const volatile unsigned int*)p + i);
+    memcpy(&r, w, sizeof(T));
+  } else {
+    unsigned char b[sizeof(T)];
+#pragma unroll
+    for (int i = 0; i < (int)sizeof(T); ++i) b[i] = *((const volatile unsigned char*)p + i);
+    memcpy(&r, b, sizeof(T));
+  }
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ void scl_st_cg(T* p, const T& v) {
+  if constexpr (sizeof(T) % 4 == 0) {
+    unsigned int w[sizeof(T) / 4];
+    memcpy(w, &v, sizeof(T));
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(T) / 4); ++i) *((volatile unsigned int*)p + i) = w[i];
+  } else {
+    unsigned char b[sizeof(T)];
+    memcpy(b, &v, sizeof(T));
+#pragma unroll
+    for (int i = 0; i < (int)sizeof(T); ++i) *((volatile unsigned char*)p + i) = b[i];
+  }
+}
+
+#if SCL_KIND == 9
+typedef SCL_TYPE_0 scl_T;
+typedef SCL_CARRY_T scl_C;
+
+// Fold (have, value) pairs across a warp; lane 0 ends with the warp's fold.
+__device__ __forceinline__ void scl_warp_fold(bool& have, scl_C& c SCL_USER_PARAMS) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    scl_C o = scl_shfl_down(c, off);
+    bool oh = __shfl_down_sync(0xffffffffu, have ? 1 : 0, off) != 0;
+    if ((threadIdx.x & 31) + off < 32 && oh) {
+      c = have ? (scl_C)SCL_FUNC_C(c, o SCL_EXTRA_ARGS) : o;
+      have = true;
+    }
+  }
+}
+
+// Block fold; the result is valid in thread 0.
+__device__ __forceinline__ void scl_block_fold(bool& have, scl_C& c SCL_USER_PARAMS) {
+  __shared__ scl_C s_val[32];
+  __shared__ int s_have[32];
+  scl_warp_fold(have, c SCL_EXTRA_ARGS);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+  if (lane == 0) {
+    s_val[warp] = c;
+    s_have[warp] = have ? 1 : 0;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    have = lane < nwarps && s_have[lane];
+    if (have) c = s_val[lane];
+    scl_warp_fold(have, c SCL_EXTRA_ARGS);
+  }
+  __syncthreads();
+}
+
+template <int U>
+__global__ void scl_reduce_k(const scl_T* in, scl_T* out, scl_u64 n, int aligned,
+                             scl_C* partials, unsigned int* ticket,
+                             unsigned int* err SCL_EXTRA_PARAMS) {
+  SCL_EXTRA_SETUP
+  constexpr int V = scl_vec_width<sizeof(scl_T)>::value;
+  const scl_u64 tid = SCL_TID(), nth = SCL_NTH();
+  if (n == 0) {
+    if (tid == 0) out[0] = (scl_T)(SCL_IDENTITY);
+    return;
+  }
+  const scl_u64 nvec = aligned ? n / V : 0;
+  bool have = false;
+  scl_T acc;
+  scl_u64 j = tid;
+  if (j < nvec) {
+    scl_pack<scl_T, V> p = scl_load<scl_T, V>(in + j * V);
+    acc = p.v[0];
+#pragma unroll
+    for (int e = 1; e < V; ++e) acc = SCL_FUNC(acc, p.v[e] SCL_EXTRA_ARGS);
+    have = true;
+    j += nth;
+  }
+  for (; j < nvec; j += nth * U) {
+    scl_pack<scl_T, V> a[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const scl_u64 k = j + (scl_u64)u * nth;
+      if (k < nvec) a[u] = scl_load<scl_T, V>(in + k * V);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const scl_u64 k = j + (scl_u64)u * nth;
+      if (k < nvec) {
+#pragma unroll
+        for (int e = 0; e < V; ++e) acc = SCL_FUNC(acc, a[u].v[e] SCL_EXTRA_ARGS);
+      }
+    }
+  }
+  for (scl_u64 i = nvec * V + tid; i < n; i += nth) {
+    acc = have ? SCL_FUNC(acc, in[i] SCL_EXTRA_ARGS) : in[i];
+    have = true;
+  }
+  scl_C c;
+  if (have) c = (scl_C)acc;
+  scl_block_fold(have, c SCL_EXTRA_ARGS);
+
+  __shared__ int s_last;
+  if (threadIdx.x == 0) {
+    // every block holds at least one element (the host sizes the grid so)
+    scl_st_cg(&partials[blockIdx.x], c);
+    __threadfence();
+    const unsigned int t = atomicAdd(ticket, 1u);
+    s_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  have = false;
+  for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+    scl_C v = scl_ld_cg(&partials[b]);
+    c = have ? (scl_C)SCL_FUNC_C(c, v SCL_EXTRA_ARGS) : v;
+    have = true;
+  }
+  scl_block_fold(have, c SCL_EXTRA_ARGS);
+  if (threadIdx.x == 0) {
+    out[0] = (scl_T)c;
+    *ticket = 0u;  // ready for the next launch on this workspace
+  }
+}
+#endif
