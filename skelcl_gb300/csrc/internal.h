@@ -9,6 +9,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -93,6 +94,9 @@ bool parse_function(const std::string& src, const std::string& name, FuncSig* si
 std::string rename_identifier(const std::string& src, const std::string& from,
                               const std::string& to);
 bool source_uses_workitem(const std::string& src);
+// Adds `#pragma unroll` before every for-loop of function `name` (a hint
+// only: the loops keep their meaning).
+std::string unroll_loops_in(const std::string& src, const std::string& name);
 std::string sha1_hex(const void* data, size_t n);
 
 // ---- programs -----------------------------------------------------------------
@@ -116,14 +120,16 @@ struct scl_program {
   size_t n_reduce_extra = 0;                // AllPairs: how many of `extra` belong to the Reduce
   std::vector<size_t> type_sizes;           // sizeof SCL_TYPE_n (read from the module)
   size_t carry_size = 0;                    // sizeof SCL_CARRY_T (Reduce / Scan)
+  int status_mode = 0;                      // Scan tile-status encoding (see scan.cuh)
   std::vector<std::string> type_names;
   bool uses_workitem = false;
   bool f64_carry = false;
   bool tc_eligible = false;                 // AllPairs: zip == x*y, reduce == x+y, id 0, float
   int overlap_range = 0;
   int padding = 0;
-  CUmodule module = nullptr;
+  std::vector<CUmodule> modules;            // the first holds scl_type_sizes
   std::map<std::string, scl::Kernel> kernels;  // by template name expression
+  std::set<std::string> lazy;               // variants compiled on first use
   scl::Workspace ws;
   uint32_t last_variant = 0;
 };

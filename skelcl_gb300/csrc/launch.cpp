@@ -126,7 +126,7 @@ int pack_extra(scl_program* p, CUfunction fn, size_t fixed, const unsigned char*
 }
 
 int launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, ArgPack& pack) {
-  if (smem > 48 * 1024) {
+  if (smem > 32 * 1024) {  // beyond the default dynamic limit once static smem is counted
     CUresult r = rt().drv.cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
                                              (int)smem);
     if (r != CUDA_SUCCESS) return cu_fail(r, "cuFuncSetAttribute(max dynamic smem)");
@@ -327,27 +327,53 @@ extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const*
   if (n == 0) return SCL_OK;
   const size_t tsz = p->type_sizes[0], csz = p->carry_size ? p->carry_size : tsz;
   const int V = vec_width(tsz);
-  uint32_t R = (tu && tu->items) ? tu->items : 4;
-  if (R != 2 && R != 4) R = 4;
+  unsigned int flags = sh->flags & (SCL_SHAPE_INCLUSIVE | SCL_SHAPE_REVERSE);
+  const bool reverse = (flags & SCL_SHAPE_REVERSE) != 0;
+  int aligned = (aligned16(in) && aligned16(out)) ? 1 : 0;
+  (void)reverse;
+  // 32 KB tiles by default: fewer tiles to look back over (measured on GB300)
+  uint32_t R = (tu && tu->items) ? tu->items : 8;
+  if (R != 2 && R != 4 && R != 8) R = 8;
   const uint64_t tile = (uint64_t)R * 256 * V;
   const uint64_t tiles = (n + tile - 1) / tile;
   if (tiles > 0x7fffffffull) return fail(SCL_ERR_ARG, "scan input too large");
-  std::string kname = "scl_scan_k<" + std::to_string(R) + ">";
+  // resident tiles per SM the register budget is sized for
+  uint32_t minb = (tu && tu->tile_w) ? tu->tile_w : (R == 8 ? 4 : (R == 4 ? 6 : 8));
+  if (!((R == 8 && (minb == 2 || minb == 3 || minb == 4)) || (R == 4 && (minb == 4 || minb == 6)) ||
+        (R == 2 && minb == 8)))
+    minb = R == 8 ? 4 : (R == 4 ? 6 : 8);
+  const std::string kname = "scl_scan_k<" + std::to_string(R) + ", " + std::to_string(minb) + ">";
   CUfunction fn = find_kernel(p, kname);
   if (!fn) return fail(SCL_ERR_LAUNCH, "kernel " + kname + " missing");
-  const size_t status_bytes = ((tiles + 1) * 4 + 255) / 256 * 256;
-  const size_t agg_bytes = (tiles * csz + 255) / 256 * 256;
-  if (int st = ensure_workspace(p, status_bytes + 2 * agg_bytes)) return st;
-  void* status = p->ws.ptr;
-  void* agg = (char*)p->ws.ptr + status_bytes;
-  void* incl = (char*)p->ws.ptr + status_bytes + agg_bytes;
-  SCL_CUDA(cudaMemsetAsync(status, 0, (tiles + 1) * 4, rt().stream));
-  unsigned int flags = sh->flags & (SCL_SHAPE_INCLUSIVE | SCL_SHAPE_REVERSE);
-  int aligned = (aligned16(in) && aligned16(out)) ? 1 : 0;
+  // workspace: [tile counter | status words / flags | values], zeroed by one memset
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  struct StatusArgs {
+    void* slots;
+    void* flags;
+    void* agg;
+    void* incl;
+  } sargs = {nullptr, nullptr, nullptr, nullptr};
+  size_t clear_bytes, total;
+  if (p->status_mode != 0) {
+    clear_bytes = 256 + up(tiles * 128);  // one 128-byte line per tile slot
+    total = clear_bytes;
+    if (int st = ensure_workspace(p, total)) return st;
+    sargs.slots = (char*)p->ws.ptr + 256;
+  } else {
+    const size_t fl = up(tiles * 4), vals = up(tiles * csz);
+    clear_bytes = 256 + fl;
+    total = clear_bytes + 2 * vals;
+    if (int st = ensure_workspace(p, total)) return st;
+    sargs.flags = (char*)p->ws.ptr + 256;
+    sargs.agg = (char*)p->ws.ptr + 256 + fl;
+    sargs.incl = (char*)p->ws.ptr + 256 + fl + vals;
+  }
+  void* counter = p->ws.ptr;
+  SCL_CUDA(cudaMemsetAsync(p->ws.ptr, 0, clear_bytes, rt().stream));
   unsigned int spin = spin_of(tu);
   unsigned int* err = rt().dev_err;
   ArgPack pack;
-  pack.ptrs = {&in, &out, &n, &flags, &aligned, &status, &agg, &incl, &spin, &err};
+  pack.ptrs = {&in, &out, &n, &flags, &aligned, &counter, &sargs, &spin, &err};
   if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
     return st;
   p->last_variant = SCL_VARIANT_VECTOR;
@@ -365,23 +391,30 @@ extern "C" int scl_launch_mapoverlap(scl_program* p, const scl_shape* sh, void* 
   if (rows == 0 || cols == 0) return SCL_OK;
   if (rows > 0x7fffffffull || cols > 0x7fffffffull) return fail(SCL_ERR_ARG, "matrix too large");
   const size_t tsz = p->type_sizes[0];
-  const int R = p->overlap_range, PY = 4, TW = 32, TH = 8 * PY;
+  const bool want_tma = !(tu && tu->variant == SCL_VARIANT_LDST);
+  int PY = (tu && tu->tile_h) ? (int)tu->tile_h : 8;  // output rows per thread
+  if (PY != 4 && PY != 8 && PY != 16) PY = 8;
+  const int R = p->overlap_range, TW = 32;
   const int xal = tsz <= 16 ? (int)std::max<size_t>(1, 16 / tsz) : 1;
   const int xlead = (R + xal - 1) / xal * xal;
   const int win_w = (xlead + TW + R + xal - 1) / xal * xal;
+  const bool tma_shape_ok = (tsz == 1 || tsz == 2 || tsz == 4 || tsz == 8) &&
+                            (cols * tsz) % 16 == 0 && aligned16(in) && win_w <= 256;
+  if (PY == 16 && !(want_tma && tma_shape_ok)) PY = 8;  // 16 rows only in the TMA form
+  if (8 * PY + 2 * R > 256 && PY > 4) PY = 4;
+  const int TH = 8 * PY;
   const int win_h = TH + 2 * R;
   const size_t win_bytes = (size_t)win_w * win_h * tsz;
   if (win_bytes > rt().smem_optin) return fail(SCL_ERR_ARG, "overlap range too large for shared memory");
   dim3 grid((unsigned)((cols + TW - 1) / TW), (unsigned)((rows + TH - 1) / TH)), block(32, 8);
   if (grid.y > 65535) return fail(SCL_ERR_ARG, "matrix has too many rows for one launch");
-  const bool want_tma = !(tu && tu->variant == SCL_VARIANT_LDST);
-  const bool tma_ok = (tsz == 1 || tsz == 2 || tsz == 4 || tsz == 8) && (cols * tsz) % 16 == 0 &&
-                      aligned16(in) && win_w <= 256 && win_h <= 256;
+  const bool tma_ok = tma_shape_ok && win_h <= 256;
+  const std::string py = "<" + std::to_string(PY) + ">";
   unsigned int spin = spin_of(tu);
   unsigned int* err = rt().dev_err;
   if (want_tma && tma_ok) {
-    CUfunction fn = find_kernel(p, "scl_mapoverlap_tma");
-    if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_mapoverlap_tma missing");
+    CUfunction fn = find_kernel(p, "scl_mapoverlap_tma" + py);
+    if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_mapoverlap_tma" + py + " missing");
     alignas(64) CUtensorMap tmap;
     CUtensorMapDataType dt = tsz == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8
                            : tsz == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16
@@ -403,8 +436,8 @@ extern "C" int scl_launch_mapoverlap(scl_program* p, const scl_shape* sh, void* 
     p->last_variant = SCL_VARIANT_TMA;
     return launch(fn, grid, block, win_bytes, pack);
   }
-  CUfunction fn = find_kernel(p, "scl_mapoverlap_ldst");
-  if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_mapoverlap_ldst missing");
+  CUfunction fn = find_kernel(p, "scl_mapoverlap_ldst" + py);
+  if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_mapoverlap_ldst" + py + " missing");
   ArgPack pack;
   pack.ptrs = {&in, &out, &rows, &cols};
   if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))

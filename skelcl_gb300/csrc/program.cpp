@@ -129,7 +129,8 @@ bool neutral_is_zero(const std::string& s) {
 
 struct Assembly {
   std::string source;
-  std::vector<std::string> kernels;  // name expressions
+  std::vector<std::string> kernels;  // name expressions compiled at construction
+  std::vector<std::string> lazy;     // further variants, compiled on first use
 };
 
 int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly* out,
@@ -160,7 +161,6 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
       << "#define SCL_PADDING " << (d->padding == SCL_PAD_NEAREST ? 1 : 0) << "\n"
       << "#define SCL_NEUTRAL (" << neutral << ")\n"
       << "#define SCL_NEUTRAL_IS_ZERO " << (neutral_is_zero(neutral) ? 1 : 0) << "\n"
-      << "#define SCL_PY 4\n"
       << scl_tpl_mapoverlap_pre << "\n";
   }
   if (kind == SCL_KIND_ALLPAIRS_GENERIC) s << scl_tpl_allpairs_pre << "\n";
@@ -220,6 +220,9 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
     const char* target = (kind == SCL_KIND_MAPOVERLAP || kind == SCL_KIND_ALLPAIRS_GENERIC)
                              ? "USR_FUNC" : "SCL_FUNC";
     std::string renamed = rename_identifier(src, func, target);
+    // Stencil taps: unrolled loops let the compiler read each staged input and
+    // each weight once per thread across the rows it computes.
+    if (kind == SCL_KIND_MAPOVERLAP) renamed = unroll_loops_in(renamed, target);
     s << "// ---- user source\n" << renamed << "\n";
     p->uses_workitem = source_uses_workitem(src);
     if (want_f64) {
@@ -260,11 +263,15 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
       break;
     case SCL_KIND_SCAN:
       s << scl_tpl_reduce << "\n" << scl_tpl_scan;
-      out->kernels = {"scl_scan_k<2>", "scl_scan_k<4>"};
+      out->kernels = {"scl_scan_k<8, 4>"};
+      out->lazy = {"scl_scan_k<8, 3>", "scl_scan_k<8, 2>", "scl_scan_k<4, 4>", "scl_scan_k<4, 6>",
+                   "scl_scan_k<2, 8>"};
       break;
     case SCL_KIND_MAPOVERLAP:
       s << scl_tpl_mapoverlap;
-      out->kernels = {"scl_mapoverlap_ldst", "scl_mapoverlap_tma"};
+      out->kernels = {"scl_mapoverlap_tma<8>"};
+      out->lazy = {"scl_mapoverlap_ldst<4>", "scl_mapoverlap_tma<4>", "scl_mapoverlap_ldst<8>",
+                   "scl_mapoverlap_tma<16>"};
       break;
     case SCL_KIND_ALLPAIRS:
       s << scl_tpl_allpairs;
@@ -279,10 +286,11 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
       return SCL_ERR_ARG;
   }
   // element / carry sizes, read back by the host after the module loads
-  s << "\nextern \"C\" __device__ const unsigned int scl_type_sizes[4] = {";
+  s << "\nextern \"C\" __device__ const unsigned int scl_type_sizes[5] = {";
   for (int i = 0; i < 3; ++i)
     s << (i < d->n_types ? "(unsigned int)sizeof(SCL_TYPE_" + std::to_string(i) + ")" : std::string("0u")) << ", ";
   s << ((kind == SCL_KIND_REDUCE || kind == SCL_KIND_SCAN) ? "(unsigned int)sizeof(SCL_CARRY_T)" : "0u")
+    << ", " << (kind == SCL_KIND_SCAN ? "(unsigned int)scl_status_mode<SCL_CARRY_T>::value" : "0u")
     << "};\n";
   out->source = s.str();
   return SCL_OK;
@@ -390,10 +398,75 @@ void copy_log(const std::string& s, char* log, size_t cap) {
   log[n] = '\0';
 }
 
+// Compile `names` out of `source` (or take them from the in-process / on-disk
+// cache).  The cache key covers the source, the options and the names.
+int compile_cached(const std::string& source, const std::vector<std::string>& names,
+                   std::string* cubin, std::map<std::string, std::string>* lowered,
+                   std::string* nvlog, std::string* hash) {
+  std::string k = source;
+  for (int i = 0; i < kNvrtcOptCount; ++i) k += std::string("\n") + kNvrtcOpts[i];
+  for (auto& n : names) k += "\n#name " + n;
+  const std::string key = sha1_hex(k.data(), k.size());
+  if (hash) *hash = sha1_hex(source.data(), source.size());
+  {
+    std::lock_guard<std::mutex> g(g_cache_mu);
+    auto it = g_mem_cache.find(key);
+    if (it != g_mem_cache.end()) {
+      *cubin = it->second.first;
+      *lowered = it->second.second;
+      return SCL_OK;
+    }
+  }
+  if (env_yes("SKELCL_LOAD_BINARY") && load_disk(key, cubin, lowered)) {
+    std::lock_guard<std::mutex> g(g_cache_mu);
+    g_mem_cache[key] = {*cubin, *lowered};
+    return SCL_OK;
+  }
+  Assembly a;
+  a.source = source;
+  a.kernels = names;
+  lowered->clear();
+  int st = nvrtc_compile(a, cubin, lowered, nvlog);
+  if (env_yes("SKELCL_PRINT_BUILD_LOG") && !nvlog->empty())
+    std::fprintf(stderr, "[skelcl] NVRTC build log:\n%s\n", nvlog->c_str());
+  if (st != SCL_OK) return st;
+  std::lock_guard<std::mutex> g(g_cache_mu);
+  g_mem_cache[key] = {*cubin, *lowered};
+  if (env_yes("SKELCL_SAVE_BINARY")) save_disk(key, *cubin, *lowered);
+  return SCL_OK;
+}
+
+int load_module(scl_program* p, const std::string& cubin,
+                const std::map<std::string, std::string>& lowered) {
+  Driver& drv = rt().drv;
+  CUmodule mod = nullptr;
+  CUresult r = drv.cuModuleLoadData(&mod, cubin.data());
+  if (r != CUDA_SUCCESS) return cu_fail(r, "cuModuleLoadData");
+  p->modules.push_back(mod);
+  for (auto& kv : lowered) {
+    CUfunction fn = nullptr;
+    r = drv.cuModuleGetFunction(&fn, mod, kv.second.c_str());
+    if (r != CUDA_SUCCESS) return cu_fail(r, ("cuModuleGetFunction " + kv.first).c_str());
+    p->kernels[kv.first] = Kernel{fn, kv.second};
+  }
+  return SCL_OK;
+}
+
 }  // namespace
 
 CUfunction find_kernel(scl_program* p, const std::string& name) {
   auto it = p->kernels.find(name);
+  if (it != p->kernels.end()) return it->second.fn;
+  if (!p->lazy.count(name)) return nullptr;
+  // variant compiled on first use (same generated source, one instantiation)
+  std::string cubin, nvlog, hash;
+  std::map<std::string, std::string> lowered;
+  if (compile_cached(p->source, {name}, &cubin, &lowered, &nvlog, &hash) != SCL_OK) {
+    fail(SCL_ERR_COMPILE, "NVRTC compilation of " + name + " failed:\n" + nvlog);
+    return nullptr;
+  }
+  if (load_module(p, cubin, lowered) != SCL_OK) return nullptr;
+  it = p->kernels.find(name);
   return it == p->kernels.end() ? nullptr : it->second.fn;
 }
 
@@ -473,70 +546,37 @@ extern "C" int scl_program_build(const scl_program_desc* desc, scl_program** out
       copy_log(err, log, log_cap);
       return fail(st, err);
     }
-    std::string key;
-    {
-      std::string k = a.source;
-      for (int i = 0; i < kNvrtcOptCount; ++i) k += std::string("\n") + kNvrtcOpts[i];
-      key = sha1_hex(k.data(), k.size());
-    }
-    p->hash = key;
-    bool have = false;
-    {
-      std::lock_guard<std::mutex> g(g_cache_mu);
-      auto it = g_mem_cache.find(key);
-      if (it != g_mem_cache.end()) {
-        cubin = it->second.first;
-        lowered = it->second.second;
-        have = true;
-      }
-    }
-    if (!have && env_yes("SKELCL_LOAD_BINARY")) have = load_disk(key, &cubin, &lowered);
-    if (!have) {
-      lowered.clear();
-      st = nvrtc_compile(a, &cubin, &lowered, &nvlog);
-      if (env_yes("SKELCL_PRINT_BUILD_LOG") && !nvlog.empty())
-        std::fprintf(stderr, "[skelcl] NVRTC build log:\n%s\n", nvlog.c_str());
-      if (st != SCL_OK) {
-        if (f64) continue;  // retry with carries in the element type
-        std::string msg = "NVRTC compilation failed:\n" + nvlog;
-        copy_log(msg, log, log_cap);
-        return fail(SCL_ERR_COMPILE, msg);
-      }
-      std::lock_guard<std::mutex> g(g_cache_mu);
-      g_mem_cache[key] = {cubin, lowered};
-      if (env_yes("SKELCL_SAVE_BINARY")) save_disk(key, cubin, lowered);
+    st = compile_cached(a.source, a.kernels, &cubin, &lowered, &nvlog, &p->hash);
+    if (st != SCL_OK) {
+      if (f64) continue;  // retry with carries in the element type
+      std::string msg = "NVRTC compilation failed:\n" + nvlog;
+      copy_log(msg, log, log_cap);
+      return fail(SCL_ERR_COMPILE, msg);
     }
     p->f64_carry = f64;
     break;
   }
   p->source = a.source;
+  for (auto& k : a.lazy) p->lazy.insert(k);
   if (int st = require_init()) {
     copy_log("scl_init() has not been called", log, log_cap);
     return st;
   }
-  Driver& drv = rt().drv;
-  CUresult r = drv.cuModuleLoadData(&p->module, cubin.data());
-  if (r != CUDA_SUCCESS) {
-    std::string msg = "cuModuleLoadData failed";
-    copy_log(msg, log, log_cap);
-    return cu_fail(r, "cuModuleLoadData");
-  }
-  for (auto& kv : lowered) {
-    CUfunction fn = nullptr;
-    r = drv.cuModuleGetFunction(&fn, p->module, kv.second.c_str());
-    if (r != CUDA_SUCCESS) return cu_fail(r, ("cuModuleGetFunction " + kv.first).c_str());
-    p->kernels[kv.first] = Kernel{fn, kv.second};
+  if (int st = load_module(p.get(), cubin, lowered)) {
+    copy_log(scl_last_error_string(), log, log_cap);
+    return st;
   }
   {
     CUdeviceptr gp = 0;
     size_t gsz = 0;
-    r = drv.cuModuleGetGlobal(&gp, &gsz, p->module, "scl_type_sizes");
+    CUresult r = rt().drv.cuModuleGetGlobal(&gp, &gsz, p->modules.front(), "scl_type_sizes");
     if (r != CUDA_SUCCESS) return cu_fail(r, "cuModuleGetGlobal(scl_type_sizes)");
-    unsigned int sz[4] = {0, 0, 0, 0};
+    unsigned int sz[5] = {0, 0, 0, 0, 0};
     cudaError_t e = cudaMemcpy(sz, (const void*)gp, sizeof(sz), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(scl_type_sizes)");
     for (int i = 0; i < desc->n_types; ++i) p->type_sizes.push_back(sz[i]);
     p->carry_size = sz[3];
+    p->status_mode = (int)sz[4];
   }
   if (log && log_cap) copy_log(nvlog, log, log_cap);
   *out = p.release();
@@ -578,7 +618,7 @@ extern "C" int scl_program_release(scl_program* p) {
   if (rt().initialized) {
     cudaStreamSynchronize(rt().stream);
     if (p->ws.ptr) cudaFree(p->ws.ptr);
-    if (p->module) rt().drv.cuModuleUnload(p->module);
+    for (CUmodule m : p->modules) rt().drv.cuModuleUnload(m);
   }
   delete p;
   return SCL_OK;

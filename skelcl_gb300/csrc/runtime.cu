@@ -54,7 +54,7 @@ template <typename F>
 int resolve(const char* sym, F* fn) {
   void* p = nullptr;
   cudaDriverEntryPointQueryResult q;
-  cudaError_t e = cudaGetDriverEntryPointByVersion(sym, &p, 12000, cudaEnableDefault, &q);
+  cudaError_t e = cudaGetDriverEntryPointByVersion(sym, &p, CUDA_VERSION, cudaEnableDefault, &q);
   if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
     return fail(SCL_ERR_CUDA, std::string("driver entry point not found: ") + sym);
   *fn = reinterpret_cast<F>(p);

@@ -291,6 +291,25 @@ std::string rename_identifier(const std::string& src, const std::string& from,
   return out;
 }
 
+std::string unroll_loops_in(const std::string& src, const std::string& name) {
+  FuncSig sig;
+  std::string err;
+  if (!parse_function(src, name, &sig, &err)) return src;
+  std::vector<Tok> t = tokenize(src);
+  std::string out;
+  size_t last = 0;
+  for (auto& k : t) {
+    if (k.b < sig.def_begin || k.e > sig.def_end) continue;
+    if (k.kind == Tok::Ident && text(src, k) == "for") {
+      out.append(src, last, k.b - last);
+      out += "\n#pragma unroll\n";
+      last = k.b;
+    }
+  }
+  out.append(src, last, std::string::npos);
+  return out;
+}
+
 bool source_uses_workitem(const std::string& src) {
   static const char* words[] = {"get_global_id", "get_local_id", "get_group_id",
                                 "get_local_size", "get_num_groups", "get_global_size",

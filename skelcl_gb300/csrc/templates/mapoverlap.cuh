@@ -12,25 +12,28 @@
 // Here both axes are padded in-kernel; no padded copy of the matrix exists.
 //
 // Shape: a block of 32 x 8 threads owns a 32-column x (8*PY)-row output tile
-// and stages the (8*PY+2R) x (TWS) input window in shared memory, either with
-// one TMA 2D tile load (OOB elements filled with zero, then patched for
+// and stages the (8*PY+2R) x SCL_WIN_W input window in shared memory, either
+// with one TMA 2D tile load (OOB elements filled with zero, then patched for
 // NEAREST / non-zero NEUTRAL) or with cooperative coalesced loads.  Each
-// thread computes PY vertically adjacent outputs so that taps shared between
-// them are loaded from shared memory once.
+// thread computes PY vertically adjacent outputs; with the user loops
+// unrolled, taps shared between those outputs and the user's weight loads
+// are read once per thread instead of once per output.
 // Generated names: SCL_OVERLAP_RANGE, SCL_PADDING (0 neutral, 1 nearest),
-// SCL_NEUTRAL, SCL_PY.
+// SCL_NEUTRAL, SCL_NEUTRAL_IS_ZERO.
 // ---------------------------------------------------------------------------
 #if SCL_KIND == 11
+
 __device__ __forceinline__ scl_u64 scl_clampi(long long v, long long hi) {
   return (scl_u64)(v < 0 ? 0 : (v > hi ? hi : v));
 }
 
 // Fill the positions of the window that lie outside the matrix.
+template <int WIN_H>
 __device__ __forceinline__ void scl_patch_border(SCL_TYPE_0* win, long long x_org, long long y_org,
                                                  scl_u64 rows, scl_u64 cols) {
   const int nthreads = blockDim.x * blockDim.y;
   const int t = threadIdx.y * blockDim.x + threadIdx.x;
-  for (int k = t; k < SCL_WIN_H * SCL_WIN_W; k += nthreads) {
+  for (int k = t; k < WIN_H * SCL_WIN_W; k += nthreads) {
     const int ly = k / SCL_WIN_W, lx = k % SCL_WIN_W;
     const long long gy = y_org + ly, gx = x_org + lx;
     const bool inside = gy >= 0 && gy < (long long)rows && gx >= 0 && gx < (long long)cols;
@@ -46,15 +49,16 @@ __device__ __forceinline__ void scl_patch_border(SCL_TYPE_0* win, long long x_or
   }
 }
 
+template <int PY>
 __device__ __forceinline__ void scl_compute_tile(const SCL_TYPE_0* win, SCL_TYPE_1* out,
                                                  scl_u64 rows, scl_u64 cols, scl_u64 x0,
                                                  scl_u64 y0 SCL_USER_PARAMS) {
   const int tx = threadIdx.x, ty = threadIdx.y;
   const scl_u64 x = x0 + tx;
-  SCL_TYPE_1 res[SCL_PY];
+  SCL_TYPE_1 res[PY];
 #pragma unroll
-  for (int p = 0; p < SCL_PY; ++p) {
-    const int ly = ty * SCL_PY + p;
+  for (int p = 0; p < PY; ++p) {
+    const int ly = ty * PY + p;
     input_matrix_t m;
     m.data = win + (ly + SCL_R) * SCL_WIN_W + SCL_XLEAD + tx;
     m.local_row = ly;
@@ -62,23 +66,25 @@ __device__ __forceinline__ void scl_compute_tile(const SCL_TYPE_0* win, SCL_TYPE
     res[p] = USR_FUNC(m SCL_EXTRA_ARGS);
   }
 #pragma unroll
-  for (int p = 0; p < SCL_PY; ++p) {
-    const scl_u64 y = y0 + ty * SCL_PY + p;
+  for (int p = 0; p < PY; ++p) {
+    const scl_u64 y = y0 + ty * PY + p;
     if (y < rows && x < cols) out[y * cols + x] = res[p];
   }
 }
 
 // Cooperative-load variant: any shape, any alignment.
-extern "C" __global__ void __launch_bounds__(256)
+template <int PY>
+__global__ void __launch_bounds__(256)
 scl_mapoverlap_ldst(const SCL_TYPE_0* in, SCL_TYPE_1* out, scl_u64 rows, scl_u64 cols
                     SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
-  SCL_TYPE_0* win = reinterpret_cast<SCL_TYPE_0*>(scl_dyn_smem);  // SCL_WIN_H x SCL_WIN_W
-  const scl_u64 x0 = (scl_u64)blockIdx.x * SCL_TW, y0 = (scl_u64)blockIdx.y * SCL_TH;
+  constexpr int TH = 8 * PY, WIN_H = TH + 2 * SCL_R;
+  SCL_TYPE_0* win = reinterpret_cast<SCL_TYPE_0*>(scl_dyn_smem);  // WIN_H x SCL_WIN_W
+  const scl_u64 x0 = (scl_u64)blockIdx.x * SCL_TW, y0 = (scl_u64)blockIdx.y * TH;
   const long long x_org = (long long)x0 - SCL_XLEAD, y_org = (long long)y0 - SCL_R;
   const int nthreads = blockDim.x * blockDim.y;
   const int t = threadIdx.y * blockDim.x + threadIdx.x;
-  for (int k = t; k < SCL_WIN_H * SCL_WIN_W; k += nthreads) {
+  for (int k = t; k < WIN_H * SCL_WIN_W; k += nthreads) {
     const int ly = k / SCL_WIN_W, lx = k % SCL_WIN_W;
     const long long gy = y_org + ly, gx = x_org + lx;
     SCL_TYPE_0 v;
@@ -94,7 +100,7 @@ scl_mapoverlap_ldst(const SCL_TYPE_0* in, SCL_TYPE_1* out, scl_u64 rows, scl_u64
     win[k] = v;
   }
   __syncthreads();
-  scl_compute_tile(win, out, rows, cols, x0, y0 SCL_EXTRA_ARGS);
+  scl_compute_tile<PY>(win, out, rows, cols, x0, y0 SCL_EXTRA_ARGS);
 }
 
 // TMA variant: one elected thread loads the whole window with
@@ -103,17 +109,20 @@ scl_mapoverlap_ldst(const SCL_TYPE_0* in, SCL_TYPE_1* out, scl_u64 rows, scl_u64
 // rule) and a 16-byte aligned base; the host checks both.
 struct __align__(64) scl_tmap { unsigned long long v[16]; };
 
-extern "C" __global__ void __launch_bounds__(256)
+template <int PY>
+__global__ void __launch_bounds__(256)
 scl_mapoverlap_tma(const __grid_constant__ scl_tmap tmap, SCL_TYPE_1* out, scl_u64 rows,
                    scl_u64 cols, unsigned int spin_limit, unsigned int* err SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
-  SCL_TYPE_0* win = reinterpret_cast<SCL_TYPE_0*>(scl_dyn_smem);  // SCL_WIN_H x SCL_WIN_W
+  constexpr int TH = 8 * PY, WIN_H = TH + 2 * SCL_R;
+  SCL_TYPE_0* win = reinterpret_cast<SCL_TYPE_0*>(scl_dyn_smem);  // WIN_H x SCL_WIN_W
   __shared__ __align__(8) unsigned long long bar;
-  const scl_u64 x0 = (scl_u64)blockIdx.x * SCL_TW, y0 = (scl_u64)blockIdx.y * SCL_TH;
+  __shared__ int s_ok;
+  const scl_u64 x0 = (scl_u64)blockIdx.x * SCL_TW, y0 = (scl_u64)blockIdx.y * TH;
   const long long x_org = (long long)x0 - SCL_XLEAD, y_org = (long long)y0 - SCL_R;
   const unsigned int bar_s = (unsigned int)__cvta_generic_to_shared(&bar);
   const int t = threadIdx.y * blockDim.x + threadIdx.x;
-  constexpr unsigned int bytes = SCL_WIN_H * SCL_WIN_W * sizeof(SCL_TYPE_0);
+  constexpr unsigned int bytes = WIN_H * SCL_WIN_W * sizeof(SCL_TYPE_0);
   if (t == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar_s));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -128,10 +137,7 @@ scl_mapoverlap_tma(const __grid_constant__ scl_tmap tmap, SCL_TYPE_1* out, scl_u
         " [%0], [%1, {%2, %3}], [%4];"
         :: "r"(dst), "l"(&tmap), "r"((int)x_org), "r"((int)y_org), "r"(bar_s)
         : "memory");
-  }
-  // Bounded wait on phase 0, by thread 0 only; the verdict is block-uniform.
-  __shared__ int s_ok;
-  if (t == 0) {
+    // Bounded wait on phase 0 by thread 0 only; the verdict is block-uniform.
     unsigned int done = 0, polls = 0;
     while (!done) {
       asm volatile(
@@ -160,11 +166,11 @@ scl_mapoverlap_tma(const __grid_constant__ scl_tmap tmap, SCL_TYPE_1* out, scl_u
   __syncthreads();
   if (!s_ok) return;
   const bool border = x_org < 0 || y_org < 0 || x_org + SCL_WIN_W > (long long)cols ||
-                      y_org + SCL_WIN_H > (long long)rows;
+                      y_org + WIN_H > (long long)rows;
 #if SCL_PADDING == 1 || SCL_NEUTRAL_IS_ZERO == 0
-  if (border) scl_patch_border(win, x_org, y_org, rows, cols);
+  if (border) scl_patch_border<WIN_H>(win, x_org, y_org, rows, cols);
 #endif
   __syncthreads();
-  scl_compute_tile(win, out, rows, cols, x0, y0 SCL_EXTRA_ARGS);
+  scl_compute_tile<PY>(win, out, rows, cols, x0, y0 SCL_EXTRA_ARGS);
 }
 #endif

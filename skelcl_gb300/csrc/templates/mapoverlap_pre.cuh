@@ -5,14 +5,12 @@
 // ---------------------------------------------------------------------------
 #define SCL_R SCL_OVERLAP_RANGE
 #define SCL_TW 32
-#define SCL_TH (8 * SCL_PY)
-// TMA x coordinates are rounded down to 16 bytes: the window starts up to
-// SCL_XPAD elements left of x0 - R.
+// TMA x coordinates must be multiples of 16 bytes: the window starts
+// SCL_XLEAD >= R elements left of the tile so that x0 - SCL_XLEAD is aligned.
 #define SCL_XALIGN (16 / (int)sizeof(SCL_TYPE_0) > 0 ? 16 / (int)sizeof(SCL_TYPE_0) : 1)
-#define SCL_XLEAD (((SCL_R + SCL_XALIGN - 1) / SCL_XALIGN) * SCL_XALIGN)  // x0 - XLEAD is aligned
+#define SCL_XLEAD (((SCL_R + SCL_XALIGN - 1) / SCL_XALIGN) * SCL_XALIGN)
 #define SCL_WIN_W_RAW (SCL_XLEAD + SCL_TW + SCL_R)
 #define SCL_WIN_W (((SCL_WIN_W_RAW + SCL_XALIGN - 1) / SCL_XALIGN) * SCL_XALIGN)
-#define SCL_WIN_H (SCL_TH + 2 * SCL_R)
 
 typedef struct {
   const SCL_TYPE_0* data;  // the thread's centre element in the staged window

@@ -16,13 +16,24 @@
 //
 // Tile = R rows x 256 threads x V elements (V = 16 bytes / sizeof T), loaded
 // with coalesced 16-byte accesses: row r of the tile is one contiguous span of
-// 256*V elements, thread t holds elements [r*256*V + t*V, +V).
+// 256*V elements, thread t holds elements [r*256*V + t*V, +V).  Tiles are
+// numbered by an atomic ticket taken when a block starts, so a tile only ever
+// waits on tiles whose blocks are already running.
 // In-tile: per-thread sequential fold, warp shuffles, one warp scans the R*8
-// warp totals.  Across tiles: warp 0 publishes the tile aggregate, then looks
-// back over up to 32 predecessors per step; every wait is bounded by
-// `spin_limit` polls, after which the tile raises SCL_DEV_ERR_TIMEOUT and
-// proceeds, so a launch always terminates.  Carries across tiles are held in
-// SCL_CARRY_T (double for float element types).
+// warp totals, publishes the tile aggregate and looks back over up to 32
+// predecessors per round trip (one lane per predecessor).  Every wait is
+// bounded by `spin_limit` polls, after which the tile raises
+// SCL_DEV_ERR_TIMEOUT and proceeds, so a launch always terminates.  Carries
+// across tiles are held in SCL_CARRY_T (double for float element types).
+//
+// Tile status: one 16-byte slot {aggregate word, inclusive word} per tile,
+// each slot alone on a 128-byte line (SCL_SLOT_STRIDE words apart), so a poll
+// is one 16-byte load and publishers and pollers of different tiles never
+// share a line (measured on GB300: sharing lines cost about a third of the
+// scan's bandwidth).
+//   mode 1, carry <= 4 bytes: word = 1<<32 | value bits; 0 = not published
+//   mode 2, carry is double : word = ~(value bits); 0 = not published
+//   mode 0, other carries   : flag word (release/acquire) + separate values
 // ---------------------------------------------------------------------------
 
 #if SCL_KIND == 10
@@ -31,8 +42,49 @@ typedef SCL_CARRY_T scl_C;
 
 #define SCL_SCAN_B 256
 #define SCL_SCAN_W 8
+#define SCL_SLOT_STRIDE 16  // 64-bit words between tile slots (128 bytes)
 #define SCL_FLAG_AGG 1u
 #define SCL_FLAG_INC 2u
+
+template <typename A, typename B> struct scl_same { static constexpr bool value = false; };
+template <typename A> struct scl_same<A, A> { static constexpr bool value = true; };
+template <typename C> struct scl_status_mode {
+  static constexpr int value = sizeof(C) <= 4 ? 1 : (scl_same<C, double>::value ? 2 : 0);
+};
+
+__device__ __forceinline__ unsigned long long scl_ld_relaxed64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void scl_st_relaxed64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
+}
+
+template <typename C>
+__device__ __forceinline__ unsigned long long scl_pack_word(const C& v) {
+  if constexpr (scl_status_mode<C>::value == 1) {
+    unsigned int bits = 0;
+    memcpy(&bits, &v, sizeof(C));
+    return (1ull << 32) | bits;
+  } else {
+    unsigned long long bits;
+    memcpy(&bits, &v, 8);
+    return ~bits;  // all-ones bits (never produced by arithmetic) would read as "not published"
+  }
+}
+template <typename C>
+__device__ __forceinline__ C scl_unpack_word(unsigned long long w) {
+  C v;
+  if constexpr (scl_status_mode<C>::value == 1) {
+    unsigned int bits = (unsigned int)w;
+    memcpy(&v, &bits, sizeof(C));
+  } else {
+    const unsigned long long bits = ~w;
+    memcpy(&v, &bits, 8);
+  }
+  return v;
+}
 
 // Ordered inclusive warp scan: lane l gets x[0] + ... + x[l].
 template <typename T>
@@ -46,10 +98,51 @@ __device__ __forceinline__ T scl_warp_incl(T v SCL_USER_PARAMS) {
   return v;
 }
 
-template <int R>
-__global__ void __launch_bounds__(SCL_SCAN_B)
+// Status storage of one launch (device pointers into the workspace).
+struct scl_scan_status {
+  unsigned long long* slots;  // modes 1, 2: slot of tile t at slots[t * SCL_SLOT_STRIDE]
+  unsigned int* flags;        // mode 0
+  scl_C* agg;                 // mode 0
+  scl_C* incl;                // mode 0
+};
+
+__device__ __forceinline__ void scl_publish(const scl_scan_status& st, unsigned int tile,
+                                            bool inclusive, const scl_C& v) {
+  if constexpr (scl_status_mode<scl_C>::value != 0) {
+    scl_st_relaxed64(st.slots + (size_t)tile * SCL_SLOT_STRIDE + (inclusive ? 1 : 0),
+                     scl_pack_word(v));
+  } else {
+    scl_st_cg(inclusive ? &st.incl[tile] : &st.agg[tile], v);
+    scl_st_release(&st.flags[tile], inclusive ? SCL_FLAG_INC : SCL_FLAG_AGG);
+  }
+}
+
+// Poll predecessor `idx` until it published something (or the wait gives up).
+// Returns 2 = inclusive prefix, 1 = aggregate, 0 = gave up; value in *v.
+__device__ __forceinline__ int scl_poll(const scl_scan_status& st, long long idx,
+                                        unsigned int spin_limit, scl_C* v) {
+  unsigned int polls = 0;
+  while (true) {
+    if constexpr (scl_status_mode<scl_C>::value != 0) {
+      unsigned long long wa, wi;
+      asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];"
+                   : "=l"(wa), "=l"(wi) : "l"(st.slots + (size_t)idx * SCL_SLOT_STRIDE) : "memory");
+      if (wi != 0ull) { *v = scl_unpack_word<scl_C>(wi); return 2; }
+      if (wa != 0ull) { *v = scl_unpack_word<scl_C>(wa); return 1; }
+    } else {
+      const unsigned int f = scl_ld_acquire(&st.flags[idx]);
+      if (f == SCL_FLAG_INC) { *v = scl_ld_cg(&st.incl[idx]); return 2; }
+      if (f == SCL_FLAG_AGG) { *v = scl_ld_cg(&st.agg[idx]); return 1; }
+    }
+    if (++polls > spin_limit) return 0;
+    if (polls > 32) scl_nanosleep(32);
+  }
+}
+
+template <int R, int MINB>
+__global__ void __launch_bounds__(SCL_SCAN_B, MINB)  // MINB resident tiles per SM at least
 scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int aligned,
-           unsigned int* status, scl_C* agg, scl_C* incl, unsigned int spin_limit,
+           unsigned int* tile_counter, scl_scan_status st, unsigned int spin_limit,
            unsigned int* err SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
   constexpr int B = SCL_SCAN_B, W = SCL_SCAN_W;
@@ -57,16 +150,15 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
   constexpr int TILE = R * B * V;
   const bool inclusive = (flags & 1u) != 0, reverse = (flags & 2u) != 0;
   const scl_T ident = (scl_T)(SCL_IDENTITY);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
   __shared__ unsigned int s_tile;
   __shared__ scl_T s_wsum[R * W];
   __shared__ scl_C s_prefix;
-  const unsigned int num_tiles = (unsigned int)((n + TILE - 1) / TILE);
-  if (threadIdx.x == 0) s_tile = atomicAdd(status + num_tiles, 1u);
+  if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
   __syncthreads();
   const unsigned int tile = s_tile;
   const scl_u64 base = (scl_u64)tile * TILE;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
   // ---- load (logical order; reverse maps logical i to physical n-1-i)
   scl_T x[R][V];
@@ -106,11 +198,10 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
   }
   __syncthreads();
 
-  // ---- warp 0: scan the R*W warp totals (row-major = tile order), then the
-  //      decoupled look-back for the tile prefix
+  // ---- warp 0: exclusive prefixes of the R*W warp totals (row-major = tile
+  //      order), the tile aggregate, then the look-back for the tile prefix
   if (warp == 0) {
     scl_T carry = ident;
-    scl_T tile_agg = ident;
 #pragma unroll
     for (int c = 0; c < (R * W + 31) / 32; ++c) {
       const int q = c * 32 + lane;
@@ -118,47 +209,31 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
       scl_T vi = scl_warp_incl(v SCL_EXTRA_ARGS);
       scl_T ve = scl_shfl_up(vi, 1);
       if (lane == 0) ve = ident;
-      if (q < R * W) s_wsum[q] = SCL_FUNC(carry, ve SCL_EXTRA_ARGS);  // exclusive prefix
+      if (q < R * W) s_wsum[q] = SCL_FUNC(carry, ve SCL_EXTRA_ARGS);
       scl_T total = scl_shfl_idx(vi, 31);
       carry = SCL_FUNC(carry, total SCL_EXTRA_ARGS);
     }
-    tile_agg = carry;
-    const scl_C aggc = (scl_C)tile_agg;
+    const scl_C aggc = (scl_C)carry;
     scl_C prefix = (scl_C)ident;
-    if (tile == 0) {
-      if (lane == 0) {
-        scl_st_cg(&incl[0], aggc);
-        scl_st_release(&status[0], SCL_FLAG_INC);
-      }
-    } else {
-      if (lane == 0) {
-        scl_st_cg(&agg[tile], aggc);
-        scl_st_release(&status[tile], SCL_FLAG_AGG);
-      }
+    if (lane == 0) scl_publish(st, tile, tile == 0, aggc);
+    if (tile != 0) {
       scl_C running = (scl_C)ident;  // fold of the tiles already visited (later ones)
       long long pred = (long long)tile - 1;
       while (true) {
         const long long idx = pred - lane;
-        unsigned int f = SCL_FLAG_INC;
-        bool timed_out = false;
+        scl_C v = (scl_C)ident;
+        int kind = 2;  // beyond tile 0: nothing to add, stop here
         if (idx >= 0) {
-          unsigned int polls = 0;
-          f = scl_ld_acquire(&status[idx]);
-          while (f == 0u) {
-            if (++polls > spin_limit) { timed_out = true; break; }
-            scl_nanosleep(polls < 64 ? 32u : 256u);
-            f = scl_ld_acquire(&status[idx]);
+          kind = scl_poll(st, idx, spin_limit, &v);
+          if (kind == 0) {
+            scl_raise(err, SCL_DEV_ERR_TIMEOUT);
+            v = (scl_C)ident;
+            kind = 2;
           }
         }
-        if (timed_out) {
-          scl_raise(err, SCL_DEV_ERR_TIMEOUT);
-          f = SCL_FLAG_INC;
-        }
-        const unsigned int pmask = __ballot_sync(0xffffffffu, f == SCL_FLAG_INC);
-        const int first = pmask ? __ffs(pmask) - 1 : 32;
-        scl_C v = (scl_C)ident;
-        if (lane <= first && idx >= 0 && !timed_out)
-          v = (f == SCL_FLAG_INC) ? scl_ld_cg(&incl[idx]) : scl_ld_cg(&agg[idx]);
+        const unsigned int pmask = __ballot_sync(0xffffffffu, kind == 2);
+        const int first = pmask ? __ffs(pmask) - 1 : 31;  // nearest inclusive prefix
+        if (lane > first) v = (scl_C)ident;
         // ordered fold over lanes: higher lane = earlier tile
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
@@ -171,28 +246,27 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
         pred -= 32;
       }
       prefix = running;
-      if (lane == 0) {
-        scl_st_cg(&incl[tile], (scl_C)SCL_FUNC_C(prefix, aggc SCL_EXTRA_ARGS));
-        scl_st_release(&status[tile], SCL_FLAG_INC);
-      }
+      if (lane == 0) scl_publish(st, tile, true, (scl_C)SCL_FUNC_C(prefix, aggc SCL_EXTRA_ARGS));
     }
     if (lane == 0) s_prefix = prefix;
   }
   __syncthreads();
 
-  // ---- outputs
+  // ---- outputs (computed in place in x)
   const scl_T tile_carry = (scl_T)s_prefix;
-  scl_T y[R][V];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     scl_T lane_excl = scl_shfl_up(wincl[r], 1);
     if (lane == 0) lane_excl = ident;
     const scl_T pre = SCL_FUNC(SCL_FUNC(tile_carry, s_wsum[r * W + warp] SCL_EXTRA_ARGS),
                                lane_excl SCL_EXTRA_ARGS);
+    if (inclusive) {
 #pragma unroll
-    for (int e = 0; e < V; ++e) {
-      if (inclusive) y[r][e] = SCL_FUNC(pre, x[r][e] SCL_EXTRA_ARGS);
-      else y[r][e] = e == 0 ? pre : SCL_FUNC(pre, x[r][e - 1] SCL_EXTRA_ARGS);
+      for (int e = 0; e < V; ++e) x[r][e] = SCL_FUNC(pre, x[r][e] SCL_EXTRA_ARGS);
+    } else {
+#pragma unroll
+      for (int e = V - 1; e > 0; --e) x[r][e] = SCL_FUNC(pre, x[r][e - 1] SCL_EXTRA_ARGS);
+      x[r][0] = pre;
     }
   }
   if (full) {
@@ -202,11 +276,11 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
       scl_pack<scl_T, V> p;
       if (!reverse) {
 #pragma unroll
-        for (int e = 0; e < V; ++e) p.v[e] = y[r][e];
+        for (int e = 0; e < V; ++e) p.v[e] = x[r][e];
         scl_store<scl_T, V>(out + base + q * V, p);
       } else {
 #pragma unroll
-        for (int e = 0; e < V; ++e) p.v[V - 1 - e] = y[r][e];
+        for (int e = 0; e < V; ++e) p.v[V - 1 - e] = x[r][e];
         scl_store<scl_T, V>(out + (n - base - (q + 1) * V), p);
       }
     }
@@ -216,7 +290,7 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
 #pragma unroll
       for (int e = 0; e < V; ++e) {
         const scl_u64 i = base + ((scl_u64)r * B + threadIdx.x) * V + e;
-        if (i < n) out[reverse ? n - 1 - i : i] = y[r][e];
+        if (i < n) out[reverse ? n - 1 - i : i] = x[r][e];
       }
   }
 }

@@ -70,8 +70,8 @@ def test_map_unaligned_views(scl):
     x = np.arange(1001, dtype=np.float32)
     p = S.Program(S.KIND_MAP, "float func(float f){ return 2.0f*f; }", ["float", "float"])
     din = dev(x)
-    dout = S.DeviceArray(1001, np.float32)
-    p.launch([din.view(1, 999), dout.view(3, 999)], n=999)
+    dout = S.DeviceArray(1002, np.float32)
+    p.launch([din.view(1, 999), dout.view(3, 999)], n=999)  # views end inside both buffers
     assert np.array_equal(dout.to_numpy()[3:1002], 2 * x[1:1000])
 
 
