@@ -28,6 +28,10 @@ public:
     return std::unique_ptr<Distribution<C>>(new Distribution<C>(*this));
   }
   const DeviceList& devices() const { return globalDeviceList; }
+  // The i-th device the container lives on (always the one GPU).
+  std::shared_ptr<Device> device(size_t i) const {
+    return i < globalDeviceList.size() ? globalDeviceList[i] : std::shared_ptr<Device>();
+  }
   bool operator==(const Distribution<C>& rhs) const { return kind() == rhs.kind(); }
   bool operator!=(const Distribution<C>& rhs) const { return !(*this == rhs); }
   virtual int kind() const { return 0; }
@@ -37,19 +41,15 @@ template <typename C>
 class SingleDistribution : public Distribution<C> {
 public:
   SingleDistribution() = default;
-  explicit SingleDistribution(const std::shared_ptr<Device>& d) : _device(d) {}
+  explicit SingleDistribution(const std::shared_ptr<Device>&) {}
   template <typename U>
-  SingleDistribution(const SingleDistribution<U>& o) : _device(o.device()) {}
+  SingleDistribution(const SingleDistribution<U>&) {}
   bool isValid() const override { return true; }
   bool isSingle() const override { return true; }
   int kind() const override { return 1; }
   std::unique_ptr<Distribution<C>> clone() const override {
     return std::unique_ptr<Distribution<C>>(new SingleDistribution<C>(*this));
   }
-  std::shared_ptr<Device> device() const { return _device; }
-
-private:
-  std::shared_ptr<Device> _device;
 };
 
 template <typename C>

@@ -52,6 +52,7 @@ private:
 
 class DeviceList {
 public:
+  typedef std::shared_ptr<Device> value_type;
   typedef std::vector<std::shared_ptr<Device>>::iterator iterator;
   typedef std::vector<std::shared_ptr<Device>>::const_iterator const_iterator;
   iterator begin() { return _devices.begin(); }
@@ -63,6 +64,7 @@ public:
   std::shared_ptr<Device>& front() { return _devices.front(); }
   const std::shared_ptr<Device>& front() const { return _devices.front(); }
   std::shared_ptr<Device>& operator[](size_t i) { return _devices[i]; }
+  const std::shared_ptr<Device>& operator[](size_t i) const { return _devices[i]; }
   void clear() { _devices.clear(); }
   void push_back(std::shared_ptr<Device> d) { _devices.push_back(std::move(d)); }
 

@@ -2,7 +2,7 @@
  * skelcl_cuda.h -- the C ABI between the SkelCL C++ headers and the GB300
  * (sm_103a) runtime in libskelcl_cuda.so.
  *
- * The SkelCL header templates (include/SkelCL/*.h) call only these entry
+ * The SkelCL header templates (the headers under include/SkelCL) call only these entry
  * points.  Every function returns an int status (SCL_OK == 0); the message of
  * the last failure on the calling thread is returned by scl_last_error_string().
  * Arguments are plain pointers and sizes: no C++ or torch types cross this

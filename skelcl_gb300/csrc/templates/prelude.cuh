@@ -241,6 +241,25 @@ SCL_MATRIX_T(scl_int4, int4)
 SCL_MATRIX_T(scl_double2, double2)
 SCL_MATRIX_T(scl_double4, double4)
 #define unsigned_int_matrix_t uint_matrix_t
+#define char_MATRIX_T
+#define uchar_MATRIX_T
+#define short_MATRIX_T
+#define ushort_MATRIX_T
+#define int_MATRIX_T
+#define uint_MATRIX_T
+#define unsigned_int_MATRIX_T
+#define long_MATRIX_T
+#define ulong_MATRIX_T
+#define float_MATRIX_T
+#define double_MATRIX_T
+#define float2_MATRIX_T
+#define float4_MATRIX_T
+#define int2_MATRIX_T
+#define int4_MATRIX_T
+#define double2_MATRIX_T
+#define double4_MATRIX_T
+#define MATRIX_GET
+#define MATRIX_SET
 #define get(m, y, x) (m).data[(int)((y) * (m).col_count + (x))]
 #define set(m, y, x, v) (m).data[(int)((y) * (m).col_count + (x))] = (v)
 
