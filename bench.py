@@ -214,7 +214,7 @@ def run_gpu(args):
     dom_bytes = BYTES_SCAN if dominant == "scan" else BYTES_MAP
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     traffic = traffic_table()
-    tkey = {"scan": "scl_scan_k<4>/int32/N=2^28", "map": "scl_map_k<4>/int32/N=2^28"}[dominant]
+    tkey = {"scan": "scan_int32_2^28", "map": "map_mod_int32_2^28"}[dominant]
 
     # ---- e2e through the C ABI with pinned host buffers -----------------------------
     import ctypes
@@ -419,6 +419,75 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+CASES = ("scan_int32", "map_mod", "zip_mul", "reduce_f32", "scan_f32", "mapoverlap", "allpairs_simt",
+         "allpairs_tc", "manhattan")
+
+
+def run_case(args):
+    """One skeleton kernel, `steps` launches after `warmup`: the small cases
+    the ncu summaries under profiles/ were captured on."""
+    import oracle
+    import skelcl_gb300 as S
+    S.init(0)
+    n = args.n
+    c = args.case
+    if c in ("scan_int32", "map_mod"):
+        x = S.DeviceArray.from_numpy(oracle.mod_i32(n, 0, 1001))
+        y = S.DeviceArray(n, np.int32)
+        if c == "scan_int32":
+            p = S.Program(S.KIND_SCAN, "int func(int x, int y){ return x+y; }", ["int"], identity="0")
+            fn = lambda: p.launch([x, y], n=n, flags=S.SHAPE_INCLUSIVE)
+        else:
+            p = S.Program(S.KIND_MAP, "int func(int x){ return x % 7919; }", ["int", "int"])
+            fn = lambda: p.launch([x, y], n=n)
+        nbytes = 8 * n
+    elif c in ("zip_mul", "reduce_f32", "scan_f32"):
+        a = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 0, -1.0, 1.0))
+        b = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 1, -1.0, 1.0))
+        z = S.DeviceArray(n, np.float32)
+        if c == "zip_mul":
+            p = S.Program(S.KIND_ZIP, "float func(float x, float y){ return x*y; }", ["float"] * 3)
+            fn = lambda: p.launch([a, b, z], n=n)
+            nbytes = 12 * n
+        elif c == "reduce_f32":
+            p = S.Program(S.KIND_REDUCE, "float func(float x, float y){ return x+y; }", ["float"], identity="0")
+            fn = lambda: p.launch([a, z], n=n)
+            nbytes = 4 * n
+        else:
+            p = S.Program(S.KIND_SCAN, "float func(float x, float y){ return x+y; }", ["float"], identity="0.0f")
+            fn = lambda: p.launch([a, z], n=n, flags=S.SHAPE_INCLUSIVE)
+            nbytes = 8 * n
+    elif c == "mapoverlap":
+        side = int(round(n ** 0.5))
+        img = S.DeviceArray.from_numpy(oracle.uniform_f32(side * side, 5, 0.0, 255.0))
+        out = S.DeviceArray(side * side, np.float32)
+        w = S.DeviceArray.from_numpy(oracle.gaussian_weights(5, 2.0).ravel())
+        src = ("float func(input_matrix_t img, __global float* w) { float s = 0.0f;"
+               " for (int dy = -5; dy <= 5; ++dy) for (int dx = -5; dx <= 5; ++dx)"
+               "  s += getData(img, dx, dy) * w[(dy + 5) * 11 + (dx + 5)]; return s; }")
+        p = S.Program(S.KIND_MAPOVERLAP, src, ["float", "float"], overlap_range=5, padding=S.PAD_NEAREST)
+        fn = lambda: p.launch([img, out], rows=side, cols=side, extra=S.buffer(w))
+        nbytes = 8 * side * side
+    else:
+        side = int(round(n ** (1 / 3)))
+        K = 256 if c == "manhattan" else side
+        A = S.DeviceArray.from_numpy(oracle.normal_f32(side * K, 7))
+        B = S.DeviceArray.from_numpy(oracle.normal_f32(K * side, 8))
+        P = S.DeviceArray(side * side, np.float32)
+        zsrc = "float func(float x, float y){ return fabs(x-y); }" if c == "manhattan" else \
+            "float func(float x, float y){ return x*y; }"
+        p = S.Program(S.KIND_ALLPAIRS, "float func(float x, float y){ return x+y; }", ["float"] * 3,
+                      source2=zsrc, identity="0")
+        var = S.VARIANT_TC3XBF16 if c == "allpairs_tc" else S.VARIANT_SIMT
+        fn = lambda: p.launch([A, B, P], rows=side, cols=side, dim=K, tuning=S.Tuning(variant=var))
+        nbytes = 2 * side * side * K  # flop
+    ms = timed(S, fn, args.steps, args.warmup)
+    print(json.dumps({"case": c, "n": n, "ms": round(ms, 4),
+                      "rate": round(nbytes / ms / 1e6, 1),
+                      "unit": "GFLOP/s" if c.startswith(("allpairs", "manhattan")) else "GB/s",
+                      "launches": S.launch_count()}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -427,10 +496,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", choices=CASES, help="time one skeleton kernel (profiling)")
+    ap.add_argument("--n", type=int, default=1 << 26, help="--case size (elements)")
     args = ap.parse_args()
     if args.warmup < 1:
         args.warmup = 1
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
