@@ -1,19 +1,444 @@
-// AllPairs zip(x*y)/reduce(x+y) on the tcgen05 tensor cores (3xBF16).
-// Placeholder until the contraction kernel lands: reports "not supported" so
-// the launch falls back to the CUDA-core kernel.
+// AllPairs zip(x*y) / reduce(x+y) over float on the 5th-generation tensor
+// cores: P = A (M x K) * B (K x N), both row-major, FP32 in and out.
+//
+// Precision: "3xBF16" (Henry, Tang & Heinecke, "Leveraging the bfloat16
+// Artificial Intelligence Datatype for Higher-Precision Computations",
+// ARITH 2019).  Each FP32 operand is split into bf16 parts
+//   x = hi + mid + lo (+ O(2^-24 |x|)),  hi = bf16(x), mid = bf16(x - hi),
+//   lo = bf16(x - hi - mid)
+// and the products whose magnitude can reach FP32 precision are accumulated
+// in FP32 in tensor memory, smallest terms first:
+//   kind 6: lo*hi + hi*lo + mid*mid + mid*hi + hi*mid + hi*hi   (3 parts)
+//   kind 3: mid*hi + hi*mid + hi*hi                              (2 parts)
+// The reference's semantics (AllPairsKernel.cl:47-135: P = sum over k of
+// A[i][k]*B[k][j], identity 0) are kept; only the order of the FP32 sums
+// differs from the sequential fold of the CUDA-core kernel.
+//
+// Shape: 128 x 128 output tile per CTA.  Warp 0 (one thread) streams k-blocks
+// of 64 with TMA (3D tensor maps over the split parts, SWIZZLE_128B, one
+// mbarrier per stage); warp 1 allocates 2 x 128 TMEM columns and one thread
+// issues tcgen05.mma.kind::f16 (M=128, N=128, K=16; both operands K-major in
+// shared memory), committing each stage back to the producer.  Each k-block
+// is accumulated into one of two TMEM accumulators (ping-pong) and drained
+// by warps 2-5 with tcgen05.ld into FP32 registers, where the k-block
+// partials are summed with round-to-nearest adds.  Measured on GB300: letting
+// the tensor core chain all 1536 MMAs of K = 4096 into one accumulator gave
+// a normwise error of 2.6e-5 against FP64, growing about linearly with K (the
+// accumulator's additions are not round-to-nearest); draining per k-block
+// keeps each chain at 24 MMAs.  Every mbarrier wait is bounded; a wait that
+// gives up raises the device status word and the CTA still frees its tensor
+// memory before it returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
 #include <cstdint>
 
 #include "internal.h"
 
 namespace scl {
+namespace tc {
 
-bool allpairs_tc_supported(uint32_t, uint32_t, uint32_t, const void*, const void*, const void*) {
-  return false;
+constexpr int BM = 128;
+constexpr int BN = 128;
+constexpr int BK = 64;                           // one 128-byte swizzle row of bf16
+constexpr int TILE_BYTES = BM * BK * 2;          // 16 KB per operand part and stage
+constexpr uint32_t TMEM_COLS = 2 * BN;           // two FP32 accumulators (ping-pong)
+constexpr int THREADS = 192;                     // 6 warps
+
+// Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
+// (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits
+// 17-22, M >> 4 in bits 24-28.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+// Shared-memory matrix descriptor for a K-major SWIZZLE_128B tile whose rows
+// are 128 bytes and whose 8-row groups are 1024 bytes apart: start address
+// >> 4 (bits 0-13), leading-byte offset 1 (unused for swizzled K-major),
+// stride-byte offset 1024 >> 4 (bits 32-45), descriptor version 1 (bits
+// 46-47), layout SWIZZLE_128B = 2 (bits 61-63).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1u << 16;
+  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)1u << 46;
+  d |= (uint64_t)2u << 61;
+  return d;
 }
 
-int allpairs_tc_launch(const float*, const float*, float*, uint32_t, uint32_t, uint32_t,
-                       cudaStream_t, uint32_t, unsigned int*) {
-  return fail(SCL_ERR_UNSUPPORTED, "tensor-core AllPairs is not built");
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{ .reg .pred p; mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;"
+      " selp.u32 %0, 1, 0, p; }"
+      : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t limit) {
+  uint32_t polls = 0;
+  while (!mbar_test(bar, parity)) {
+    if (++polls > limit) return false;
+    if (polls > 64) __nanosleep(32);
+  }
+  return true;
+}
+
+__device__ __forceinline__ void raise(unsigned int* err) {
+  if (err) atomicOr(err, 1u);
+}
+
+// The split parts live in one [part][row][Kp] bf16 array per operand; rows and
+// Kp are padded to the tile sizes and zero-filled, so every TMA box is in
+// bounds.
+__global__ void split_rows_kernel(const float* __restrict__ X, uint32_t R, uint32_t C, uint32_t Rp,
+                                  uint32_t Cp, int parts, __nv_bfloat16* __restrict__ out) {
+  const uint64_t total = (uint64_t)Rp * Cp;
+  const uint64_t plane = total;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t r = (uint32_t)(i / Cp), c = (uint32_t)(i % Cp);
+    const float x = (r < R && c < C) ? X[(uint64_t)r * C + c] : 0.0f;
+    const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(hi);
+    const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+    out[i] = hi;
+    out[plane + i] = mid;
+    if (parts > 2) out[2 * plane + i] = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+  }
+}
+
+// B (K x N row-major) -> parts of B^T ([part][n][Kp]), through 32 x 32 tiles.
+__global__ void split_transpose_kernel(const float* __restrict__ B, uint32_t K, uint32_t N,
+                                       uint32_t Np, uint32_t Kp, int parts,
+                                       __nv_bfloat16* __restrict__ out) {
+  __shared__ float tile[32][33];
+  const uint32_t k0 = blockIdx.y * 32, n0 = blockIdx.x * 32;
+  const uint64_t plane = (uint64_t)Np * Kp;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const uint32_t k = k0 + j, n = n0 + threadIdx.x;
+    tile[j][threadIdx.x] = (k < K && n < N) ? B[(uint64_t)k * N + n] : 0.0f;
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const uint32_t n = n0 + j, k = k0 + threadIdx.x;
+    if (n >= Np || k >= Kp) continue;
+    const float x = tile[threadIdx.x][j];
+    const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(hi);
+    const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+    const uint64_t o = (uint64_t)n * Kp + k;
+    out[o] = hi;
+    out[plane + o] = mid;
+    if (parts > 2) out[2 * plane + o] = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+  }
+}
+
+template <int PARTS, int STAGES>
+__global__ void __launch_bounds__(THREADS, 1)
+gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   float* __restrict__ P, uint32_t M, uint32_t N, uint32_t Kp, uint32_t spin_limit,
+                   unsigned int* err) {
+  constexpr int STAGE_BYTES = 2 * PARTS * TILE_BYTES;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[STAGES];
+  __shared__ __align__(8) uint64_t acc_full[2];   // MMA -> epilogue: k-block partial ready
+  __shared__ __align__(8) uint64_t acc_empty[2];  // epilogue -> MMA: accumulator drained
+  __shared__ __align__(8) uint64_t drain_bar;     // all issued MMAs have finished
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_fail;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;  // 1024-aligned stage ring
+  const uint32_t n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
+  const uint32_t nk = Kp / BK;
+
+  if (threadIdx.x == 0) {
+    s_fail = 0;
+    for (int s = 0; s < STAGES; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&full_bar[s])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&empty_bar[s])));
+    }
+    for (int a = 0; a < 2; ++a) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&acc_full[a])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" :: "r"(smem_u32(&acc_empty[a])));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&drain_bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" :: "l"(&tmA) : "memory");
+    asm volatile("prefetch.tensormap [%0];" :: "l"(&tmB) : "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(smem_u32(&tmem_slot)), "r"(TMEM_COLS) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0) {
+    // ---- TMA producer
+    if (lane == 0) {
+      for (uint32_t kb = 0; kb < nk; ++kb) {
+        const int s = (int)(kb % STAGES);
+        const uint32_t round = kb / STAGES;
+        if (round > 0 && !mbar_wait(smem_u32(&empty_bar[s]), (round - 1) & 1u, spin_limit)) {
+          raise(err);
+          s_fail = 1;
+          break;
+        }
+        const uint32_t fb = smem_u32(&full_bar[s]);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                     :: "r"(fb), "r"((uint32_t)STAGE_BYTES) : "memory");
+        const uint32_t stage = base + (uint32_t)s * STAGE_BYTES;
+        const int kx = (int)(kb * BK);
+#pragma unroll
+        for (int p = 0; p < PARTS; ++p) {
+          asm volatile(
+              "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+              " [%0], [%1, {%2, %3, %4}], [%5];"
+              :: "r"(stage + (uint32_t)p * TILE_BYTES), "l"(&tmA), "r"(kx), "r"((int)m0), "r"(p),
+                 "r"(fb)
+              : "memory");
+          asm volatile(
+              "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+              " [%0], [%1, {%2, %3, %4}], [%5];"
+              :: "r"(stage + (uint32_t)(PARTS + p) * TILE_BYTES), "l"(&tmB), "r"(kx), "r"((int)n0),
+                 "r"(p), "r"(fb)
+              : "memory");
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer
+    if (lane == 0) {
+      // (a part, b part) products, smallest first
+      constexpr int NPROD = PARTS == 3 ? 6 : 3;
+      int prod_a[NPROD], prod_b[NPROD];
+      if (PARTS == 3) {  // lo*hi, hi*lo, mid*mid, mid*hi, hi*mid, hi*hi
+        const int pa[6] = {2, 0, 1, 1, 0, 0}, pb[6] = {0, 2, 1, 0, 1, 0};
+        for (int q = 0; q < NPROD; ++q) { prod_a[q] = pa[q]; prod_b[q] = pb[q]; }
+      } else {           // mid*hi, hi*mid, hi*hi
+        const int pa[3] = {1, 0, 0}, pb[3] = {0, 1, 0};
+        for (int q = 0; q < NPROD; ++q) { prod_a[q] = pa[q]; prod_b[q] = pb[q]; }
+      }
+      for (uint32_t kb = 0; kb < nk; ++kb) {
+        const int s = (int)(kb % STAGES);
+        const int acc_i = (int)(kb & 1u);
+        const uint32_t use = kb >> 1;  // how often this accumulator was used before
+        if (use > 0 && !mbar_wait(smem_u32(&acc_empty[acc_i]), (use - 1) & 1u, spin_limit)) {
+          raise(err);
+          s_fail = 1;
+          break;
+        }
+        if (!mbar_wait(smem_u32(&full_bar[s]), (kb / STAGES) & 1u, spin_limit)) {
+          raise(err);
+          s_fail = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t stage = base + (uint32_t)s * STAGE_BYTES;
+        const uint32_t dtm = tmem + (uint32_t)(acc_i * BN);
+#pragma unroll
+        for (int q = 0; q < NPROD; ++q) {
+          const uint64_t ad = smem_desc(stage + (uint32_t)prod_a[q] * TILE_BYTES);
+          const uint64_t bd = smem_desc(stage + (uint32_t)(PARTS + prod_b[q]) * TILE_BYTES);
+#pragma unroll
+          for (int ks = 0; ks < BK / 16; ++ks) {
+            // advance 16 bf16 = 32 bytes along K inside the swizzle row
+            const uint64_t a = ad + (uint64_t)(ks * 2);
+            const uint64_t b = bd + (uint64_t)(ks * 2);
+            const uint32_t acc = (q > 0 || ks > 0) ? 1u : 0u;  // fresh partial per k-block
+            asm volatile(
+                "{ .reg .pred p; setp.ne.b32 p, %4, 0;"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }"
+                :: "r"(dtm), "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+                : "memory");
+          }
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+            :: "r"(smem_u32(&empty_bar[s])) : "memory");
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+            :: "r"(smem_u32(&acc_full[acc_i])) : "memory");
+      }
+      // no MMA may still run when the tensor memory is freed (also after a
+      // failed wait above)
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+          :: "r"(smem_u32(&drain_bar)) : "memory");
+      if (!mbar_wait(smem_u32(&drain_bar), 0, spin_limit)) raise(err);
+    }
+  } else {
+    // ---- epilogue: warps 2..5 own TMEM lanes 32*(warp % 4) ...; each thread
+    //      keeps its row's 128 partial sums in registers
+    const int q = warp & 3;
+    float sum[BN];
+#pragma unroll
+    for (int j = 0; j < BN; ++j) sum[j] = 0.0f;
+    bool ok = true;
+    for (uint32_t kb = 0; kb < nk; ++kb) {
+      const int acc_i = (int)(kb & 1u);
+      if (!mbar_wait(smem_u32(&acc_full[acc_i]), (kb >> 1) & 1u, spin_limit)) {
+        if (lane == 0) raise(err);
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int c = 0; c < BN / 32; ++c) {
+        uint32_t r[32];
+        const uint32_t taddr =
+            tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc_i * BN + c * 32);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10,"
+            " %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27,"
+            " %28, %29, %30, %31}, [%32];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+              "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+              "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+              "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+              "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+              "=r"(r[31])
+            : "r"(taddr)
+            : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 32; ++j) sum[c * 32 + j] += __uint_as_float(r[j]);
+      }
+      // accumulator drained: hand it back to the MMA issuer (one arrive per warp)
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];"
+                     :: "r"(smem_u32(&acc_empty[acc_i])) : "memory");
+    }
+    if (ok) {
+      const uint32_t row = m0 + (uint32_t)(q * 32 + lane);
+      if (row < M) {
+        const bool vec = (N % 4u) == 0u;
+#pragma unroll
+        for (int c = 0; c < BN / 32; ++c) {
+          const uint32_t col0 = n0 + (uint32_t)(c * 32);
+          float* dst = P + (uint64_t)row * N + col0;
+          if (vec && col0 + 32 <= N) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 4)
+              *reinterpret_cast<float4*>(dst + j) =
+                  make_float4(sum[c * 32 + j], sum[c * 32 + j + 1], sum[c * 32 + j + 2],
+                              sum[c * 32 + j + 3]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if (col0 + j < N) dst[j] = sum[c * 32 + j];
+          }
+        }
+      }
+    }
+  }
+
+  // ---- teardown: wait for the copies a failed pipeline may still have in
+  //      flight (bounded), then free the tensor memory
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (s_fail && threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_wait(smem_u32(&full_bar[s]), 0, spin_limit);
+      mbar_wait(smem_u32(&full_bar[s]), 1, spin_limit);
+    }
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                 :: "r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+inline uint32_t round_up(uint32_t v, uint32_t m) { return (v + m - 1) / m * m; }
+
+}  // namespace tc
+
+size_t allpairs_tc_scratch_bytes(uint32_t M, uint32_t N, uint32_t K, int parts) {
+  const uint64_t Mp = tc::round_up(M, tc::BM), Np = tc::round_up(N, tc::BN),
+                 Kp = tc::round_up(K, tc::BK);
+  return (size_t)parts * (Mp + Np) * Kp * 2 + 1024;
+}
+
+bool allpairs_tc_supported(uint32_t M, uint32_t N, uint32_t K, const void*, const void*,
+                           const void*) {
+  // the split arrays' row pitch (Kp * 2 bytes) and plane sizes stay far below
+  // the tensor-map limits for any 32-bit shape; tiny products are not worth
+  // the split
+  return (uint64_t)M * N >= 128ull * 128ull && K >= 16 && rt().cc_major == 10;
+}
+
+static int encode_parts(CUtensorMap* tm, void* base, uint64_t rows, uint64_t Kp, int parts) {
+  cuuint64_t dims[3] = {Kp, rows, (cuuint64_t)parts};
+  cuuint64_t strides[2] = {Kp * 2, rows * Kp * 2};
+  cuuint32_t box[3] = {(cuuint32_t)tc::BK, (cuuint32_t)tc::BM, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = rt().drv.cuTensorMapEncodeTiled(
+      tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
+      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return cu_fail(r, "cuTensorMapEncodeTiled(3xbf16 parts)");
+  return SCL_OK;
+}
+
+int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uint32_t N,
+                       uint32_t K, int parts, void* scratch, size_t scratch_bytes,
+                       cudaStream_t stream, uint32_t spin_limit, unsigned int* err) {
+  if (parts != 2 && parts != 3) return fail(SCL_ERR_ARG, "3xBF16: parts must be 2 or 3");
+  const uint32_t Mp = tc::round_up(M, tc::BM), Np = tc::round_up(N, tc::BN),
+                 Kp = tc::round_up(K, tc::BK);
+  if (scratch_bytes < allpairs_tc_scratch_bytes(M, N, K, parts))
+    return fail(SCL_ERR_ARG, "3xBF16: scratch too small");
+  uint8_t* s = reinterpret_cast<uint8_t*>(((uintptr_t)scratch + 1023) & ~(uintptr_t)1023);
+  __nv_bfloat16* a_parts = reinterpret_cast<__nv_bfloat16*>(s);
+  __nv_bfloat16* b_parts = a_parts + (size_t)parts * Mp * Kp;
+
+  const int sm = rt().sm_count > 0 ? rt().sm_count : 148;
+  tc::split_rows_kernel<<<sm * 8, 256, 0, stream>>>(A, M, K, Mp, Kp, parts, a_parts);
+  dim3 tgrid((Np + 31) / 32, (Kp + 31) / 32);
+  tc::split_transpose_kernel<<<tgrid, dim3(32, 8), 0, stream>>>(B, K, N, Np, Kp, parts, b_parts);
+  rt().launches += 2;
+
+  alignas(64) CUtensorMap tmA, tmB;
+  if (int st = encode_parts(&tmA, a_parts, Mp, Kp, parts)) return st;
+  if (int st = encode_parts(&tmB, b_parts, Np, Kp, parts)) return st;
+
+  dim3 grid(Np / tc::BN, Mp / tc::BM);
+  if (grid.y > 65535) return fail(SCL_ERR_ARG, "3xBF16: too many row tiles");
+  cudaError_t e;
+  if (parts == 3) {
+    constexpr int STAGES = 2;
+    const size_t smem = (size_t)STAGES * 2 * 3 * tc::TILE_BYTES + 1024;
+    auto kern = tc::gemm_3xbf16_kernel<3, STAGES>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(3xbf16)");
+    kern<<<grid, tc::THREADS, smem, stream>>>(tmA, tmB, P, M, N, Kp, spin_limit, err);
+  } else {
+    constexpr int STAGES = 3;
+    const size_t smem = (size_t)STAGES * 2 * 2 * tc::TILE_BYTES + 1024;
+    auto kern = tc::gemm_3xbf16_kernel<2, STAGES>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(3xbf16)");
+    kern<<<grid, tc::THREADS, smem, stream>>>(tmA, tmB, P, M, N, Kp, spin_limit, err);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "3xBF16 launch");
+  rt().launches += 1;
+  return SCL_OK;
 }
 
 }  // namespace scl

@@ -12,7 +12,9 @@
 // tcgen05 contraction (allpairs_tc.cu)
 namespace scl {
 int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uint32_t N,
-                       uint32_t K, cudaStream_t stream, uint32_t spin_limit, unsigned int* err);
+                       uint32_t K, int parts, void* scratch, size_t scratch_bytes,
+                       cudaStream_t stream, uint32_t spin_limit, unsigned int* err);
+size_t allpairs_tc_scratch_bytes(uint32_t M, uint32_t N, uint32_t K, int parts);
 bool allpairs_tc_supported(uint32_t M, uint32_t N, uint32_t K, const void* A, const void* B,
                            const void* P);
 }  // namespace scl
@@ -464,9 +466,13 @@ extern "C" int scl_launch_allpairs(scl_program* p, const scl_shape* sh, void* co
     const uint32_t want = tu ? tu->variant : SCL_VARIANT_AUTO;
     if (p->tc_eligible && want != SCL_VARIANT_SIMT && extra_bytes == 0 &&
         allpairs_tc_supported(M, N, K, A, B, P)) {
+      // tuning.items == 2: two bf16 parts, 3 products; otherwise three parts, 6 products
+      const int parts = (tu && tu->items == 2) ? 2 : 3;
+      const size_t need = allpairs_tc_scratch_bytes(M, N, K, parts);
+      if (int st = ensure_workspace(p, need)) return st;
       p->last_variant = SCL_VARIANT_TC3XBF16;
-      return allpairs_tc_launch((const float*)A, (const float*)B, (float*)P, M, N, K, rt().stream,
-                                spin_of(tu), rt().dev_err);
+      return allpairs_tc_launch((const float*)A, (const float*)B, (float*)P, M, N, K, parts,
+                                p->ws.ptr, p->ws.bytes, rt().stream, spin_of(tu), rt().dev_err);
     }
     if (want == SCL_VARIANT_TC3XBF16)
       return fail(SCL_ERR_UNSUPPORTED, "the tensor-core AllPairs needs zip x*y, reduce x+y, identity 0, "
