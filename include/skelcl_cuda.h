@@ -217,6 +217,33 @@ int scl_launch_allpairs(scl_program* prog, const scl_shape* shape,
                         void* const* buffers, const void* extra,
                         size_t extra_bytes, const scl_tuning* tuning);
 
+/* ---- Scan that allocates nothing.  No counterpart in the reference.
+ *      Same arguments and results as scl_launch_scan, but the scan's scratch
+ *      (tile counter and per-tile status) is one fixed array compiled into
+ *      this library, so the call never allocates or frees device memory.
+ *      It is for callers that must not: a process whose GPU memory belongs
+ *      to another allocator (a framework's caching allocator, a server that
+ *      reserves nearly all HBM at start-up), where an allocation behind the
+ *      owner's back can fail or take memory it had counted on; and a
+ *      latency-bound loop, where cudaFree waits for the whole device.
+ *      Limit: the scratch must fit in SCL_NOALLOC_SCRATCH_BYTES (4 MiB), which
+ *      holds the status of 32766 tiles: 268,419,072 elements of int,
+ *      unsigned int or float, or 134,209,536 of double.  Longer inputs return
+ *      SCL_ERR_ARG with the limit for their element type in the message;
+ *      scl_launch_scan has no such limit.
+ *      Only the default tile shape is used (of `tuning`, only spin_limit).
+ *      Every GPU that loads this library holds the array until the process
+ *      exits.  The first call on a device looks up the array's device
+ *      address (once per device), so make that first call before any stream
+ *      capture.  All calls share the array and it keeps the last call's
+ *      contents; each call clears the part it needs before its kernel runs.
+ *      Calls that overlap on the GPU race on it (the library stream runs
+ *      its calls one after another). */
+#define SCL_NOALLOC_SCRATCH_BYTES (4u << 20)
+int scl_launch_scan_noalloc(scl_program* prog, const scl_shape* shape,
+                            void* const* buffers, const void* extra,
+                            size_t extra_bytes, const scl_tuning* tuning);
+
 /* Variant the last launch of `prog` used (SCL_VARIANT_*). */
 int scl_program_last_variant(const scl_program* prog, uint32_t* variant);
 /* Kernels this library launched since scl_init (all programs). */

@@ -93,6 +93,7 @@ SIGNATURES = {
     "scl_launch_zip": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_reduce": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_scan": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
+    "scl_launch_scan_noalloc": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_mapoverlap": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_allpairs": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_count": ([ctypes.POINTER(_U64)], _I),

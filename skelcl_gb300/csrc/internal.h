@@ -137,6 +137,21 @@ struct scl_program {
 namespace scl {
 CUfunction find_kernel(scl_program* p, const std::string& name);
 int ensure_workspace(scl_program* p, size_t bytes);
+
+// Kernel parameters of one launch (launch.cpp)
+struct ArgPack {
+  std::vector<void*> ptrs;
+  uint32_t vals[64];  // storage for values built here (Local offsets)
+  int nvals = 0;
+  size_t local_bytes = 0;
+};
+// Appends the user function's extra arguments from the ABI blob to `pack`,
+// checking them against the program's parameters; `fixed` = skeleton
+// parameters already in `pack`.
+int pack_extra(scl_program* p, CUfunction fn, size_t fixed, const unsigned char* blob,
+               size_t bytes, ArgPack* pack);
+// cuLaunchKernel on the library stream.
+int launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, ArgPack& pack);
 // Autotuner lookup/store; returns false when nothing is cached.
 bool tune_lookup(const std::string& key, scl_tuning* out);
 void tune_store(const std::string& key, const scl_tuning& t);

@@ -24,13 +24,6 @@ namespace {
 
 constexpr uint32_t kDefaultSpin = 1u << 22;  // polls; ~0.1-1 s with back-off
 
-struct ArgPack {
-  std::vector<void*> ptrs;
-  uint32_t vals[64];  // storage for values built here (Local offsets)
-  int nvals = 0;
-  size_t local_bytes = 0;
-};
-
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 const char* kind_name(uint32_t k) {
@@ -42,6 +35,8 @@ const char* kind_name(uint32_t k) {
     default: return "unknown";
   }
 }
+
+}  // namespace
 
 // Walks the blob against program parameters [first, first+count) and appends
 // kernel-parameter pointers.  `fixed` = number of skeleton kernel params
@@ -140,6 +135,8 @@ int launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, ArgPack& pack) {
   ++rt().launches;
   return SCL_OK;
 }
+
+namespace {
 
 int max_resident_blocks(CUfunction fn, int block, size_t smem) {
   int per_sm = 0;
