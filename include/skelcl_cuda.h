@@ -50,7 +50,15 @@ enum scl_kind {
   SCL_KIND_SCAN = 10,           /* T f(T, T, extra...)          ScanDef.h:70-297   */
   SCL_KIND_MAPOVERLAP = 11,     /* Tout f(input_matrix_t, ...)  MapOverlapDef.h:71-279 */
   SCL_KIND_ALLPAIRS = 12,       /* reduce + zip pair            AllPairsDef.h:77-91,213-280 */
-  SCL_KIND_ALLPAIRS_GENERIC = 13 /* Tout f(lmatrix_t*, rmatrix_t*, dim, ...) AllPairsDef.h:93-107,283-344 */
+  SCL_KIND_ALLPAIRS_GENERIC = 13, /* Tout f(lmatrix_t*, rmatrix_t*, dim, ...) AllPairsDef.h:93-107,283-344 */
+  /* Adjoints (no counterpart in the reference).  `source`/`func` give the
+   * vector-Jacobian product of the forward function; type_names are the
+   * forward's (Tin, Tout / Tl, Tr, Tout).  Launched with scl_launch_map. */
+  SCL_KIND_MAP_ADJOINT = 14,    /* Tin  d(Tin x, Tout g, extra...)            */
+  SCL_KIND_ZIP_ADJOINT = 15     /* Tl dl(Tl x, Tr y, Tout g, extra...) = func,
+                                   Tr dr(Tl x, Tr y, Tout g, extra...) = func2
+                                   (in `source`, or in `source2` if given;
+                                   same extra parameters as dl; optional) */
 };
 
 /* MapOverlap padding modes (include/SkelCL/detail/Padding.h:47-50). */
@@ -99,6 +107,12 @@ typedef struct scl_shape {
 
 #define SCL_SHAPE_INCLUSIVE 0x1u  /* Scan: inclusive instead of exclusive     */
 #define SCL_SHAPE_REVERSE   0x2u  /* Scan: scan from the end (adjoint of Scan) */
+#define SCL_SHAPE_ACCUMULATE 0x4u /* adjoint kinds: add into the first gradient
+                                     instead of overwriting it                 */
+#define SCL_SHAPE_ACCUMULATE_RIGHT 0x8u /* Zip adjoint: add into the second */
+#define SCL_SHAPE_TRANS_LEFT  0x10u /* AllPairs x*y/x+y: the left operand is
+                                       stored transposed (dim x rows)          */
+#define SCL_SHAPE_TRANS_RIGHT 0x20u /* ... the right operand (cols x dim)      */
 
 /* Launch tuning; NULL means "defaults or autotuned".  Zero fields keep their
  * default.  workgroup mirrors Skeleton::setWorkGroupSize (src/Skeleton.cpp:75-78). */
@@ -243,6 +257,22 @@ int scl_launch_allpairs(scl_program* prog, const scl_shape* shape,
 int scl_launch_scan_noalloc(scl_program* prog, const scl_shape* shape,
                             void* const* buffers, const void* extra,
                             size_t extra_bytes, const scl_tuning* tuning);
+
+/* ---- adjoint building blocks (no counterpart in the reference; used by the
+ *      reverse-mode tape in include/SkelCL/Adjoint.h).  Element types:   */
+enum scl_dtype { SCL_DTYPE_F32 = 1, SCL_DTYPE_F64 = 2 };
+/* Adjoint of Reduce(+): gx[i] = g (or gx[i] += g with `accumulate`), g read
+ * from DEVICE memory (the gradient of the reduced scalar). */
+int scl_adjoint_broadcast(const void* g, void* gx, uint64_t n, int dtype, int accumulate);
+/* dst[i] += src[i]: gradient accumulation where an adjoint cannot add itself. */
+int scl_adjoint_accumulate(void* dst, const void* src, uint64_t n, int dtype);
+/* Adjoint of a linear MapOverlap with NEAREST padding, edge part.  With
+ * w = the (2R+1)^2 transposed-stencil weights (w[(dy+R)(2R+1)+dx+R] multiplies
+ * g[y+dy][x+dx]) and gin already holding the zero-padded transposed stencil
+ * of g, adds to every edge pixel of gin what the clamped reads of the forward
+ * sent there from outside the matrix.  Float only. */
+int scl_mapoverlap_adjoint_edges(const float* g, const float* w, float* gin, uint64_t rows,
+                                 uint64_t cols, int R);
 
 /* Variant the last launch of `prog` used (SCL_VARIANT_*). */
 int scl_program_last_variant(const scl_program* prog, uint32_t* variant);

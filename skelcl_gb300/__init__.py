@@ -22,8 +22,11 @@ OK, ERR_ARG, ERR_OOM, ERR_COMPILE, ERR_LAUNCH, ERR_TIMEOUT, ERR_CUDA, ERR_NOT_IN
 KIND_MAP, KIND_MAP_VOID, KIND_MAP_INDEX, KIND_MAP_INDEX_VOID = 1, 2, 3, 4
 KIND_MAP_POINT, KIND_MAP_POINT_VOID, KIND_ZIP, KIND_ZIP_VOID = 5, 6, 7, 8
 KIND_REDUCE, KIND_SCAN, KIND_MAPOVERLAP, KIND_ALLPAIRS, KIND_ALLPAIRS_GENERIC = 9, 10, 11, 12, 13
+KIND_MAP_ADJOINT, KIND_ZIP_ADJOINT = 14, 15
 PAD_NEUTRAL, PAD_NEAREST = 0, 1
 SHAPE_INCLUSIVE, SHAPE_REVERSE = 1, 2
+SHAPE_ACCUMULATE, SHAPE_ACCUMULATE_RIGHT, SHAPE_TRANS_LEFT, SHAPE_TRANS_RIGHT = 4, 8, 16, 32
+DTYPE_F32, DTYPE_F64 = 1, 2
 VARIANT_AUTO, VARIANT_SIMPLE, VARIANT_VECTOR, VARIANT_SIMT, VARIANT_TC3XBF16, VARIANT_TMA, VARIANT_LDST = range(7)
 ARG_VALUE, ARG_BUFFER, ARG_MATRIX, ARG_LOCAL = 1, 2, 3, 4
 PROG_NO_F64_CARRY = 1
@@ -100,6 +103,9 @@ SIGNATURES = {
     "scl_graph_begin": ([], _I), "scl_graph_end": ([ctypes.POINTER(_VP)], _I),
     "scl_graph_launch": ([_VP], _I), "scl_graph_destroy": ([_VP], _I),
     "scl_debug_bounded_wait": ([_U32, ctypes.POINTER(_I)], _I),
+    "scl_adjoint_broadcast": ([_VP, _VP, _U64, _I, _I], _I),
+    "scl_adjoint_accumulate": ([_VP, _VP, _U64, _I], _I),
+    "scl_mapoverlap_adjoint_edges": ([_VP, _VP, _VP, _U64, _U64, _I], _I),
 }
 
 _LIB: Optional[ctypes.CDLL] = None
@@ -287,7 +293,8 @@ _LAUNCH = {KIND_MAP: "scl_launch_map", KIND_MAP_VOID: "scl_launch_map",
            KIND_ZIP: "scl_launch_zip", KIND_ZIP_VOID: "scl_launch_zip",
            KIND_REDUCE: "scl_launch_reduce", KIND_SCAN: "scl_launch_scan",
            KIND_MAPOVERLAP: "scl_launch_mapoverlap", KIND_ALLPAIRS: "scl_launch_allpairs",
-           KIND_ALLPAIRS_GENERIC: "scl_launch_allpairs"}
+           KIND_ALLPAIRS_GENERIC: "scl_launch_allpairs",
+           KIND_MAP_ADJOINT: "scl_launch_map", KIND_ZIP_ADJOINT: "scl_launch_map"}
 
 
 class Program:

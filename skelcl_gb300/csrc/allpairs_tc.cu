@@ -396,7 +396,7 @@ static int encode_parts(CUtensorMap* tm, void* base, uint64_t rows, uint64_t Kp,
 }
 
 int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uint32_t N,
-                       uint32_t K, int parts, void* scratch, size_t scratch_bytes,
+                       uint32_t K, int parts, int trans, void* scratch, size_t scratch_bytes,
                        cudaStream_t stream, uint32_t spin_limit, unsigned int* err) {
   if (parts != 2 && parts != 3) return fail(SCL_ERR_ARG, "3xBF16: parts must be 2 or 3");
   const uint32_t Mp = tc::round_up(M, tc::BM), Np = tc::round_up(N, tc::BN),
@@ -408,9 +408,21 @@ int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uin
   __nv_bfloat16* b_parts = a_parts + (size_t)parts * Mp * Kp;
 
   const int sm = rt().sm_count > 0 ? rt().sm_count : 148;
-  tc::split_rows_kernel<<<sm * 8, 256, 0, stream>>>(A, M, K, Mp, Kp, parts, a_parts);
-  dim3 tgrid((Np + 31) / 32, (Kp + 31) / 32);
-  tc::split_transpose_kernel<<<tgrid, dim3(32, 8), 0, stream>>>(B, K, N, Np, Kp, parts, b_parts);
+  // both operands end up K-major ([row][k] and [col][k]); a transposed
+  // operand (trans bit 0: A stored K x M, bit 1: B stored N x K) swaps which
+  // of the two split kernels produces it
+  if (trans & 1) {
+    dim3 agrid((Mp + 31) / 32, (Kp + 31) / 32);
+    tc::split_transpose_kernel<<<agrid, dim3(32, 8), 0, stream>>>(A, K, M, Mp, Kp, parts, a_parts);
+  } else {
+    tc::split_rows_kernel<<<sm * 8, 256, 0, stream>>>(A, M, K, Mp, Kp, parts, a_parts);
+  }
+  if (trans & 2) {
+    tc::split_rows_kernel<<<sm * 8, 256, 0, stream>>>(B, N, K, Np, Kp, parts, b_parts);
+  } else {
+    dim3 tgrid((Np + 31) / 32, (Kp + 31) / 32);
+    tc::split_transpose_kernel<<<tgrid, dim3(32, 8), 0, stream>>>(B, K, N, Np, Kp, parts, b_parts);
+  }
   rt().launches += 2;
 
   alignas(64) CUtensorMap tmA, tmB;

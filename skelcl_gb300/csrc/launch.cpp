@@ -12,8 +12,11 @@
 // tcgen05 contraction (allpairs_tc.cu)
 namespace scl {
 int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uint32_t N,
-                       uint32_t K, int parts, void* scratch, size_t scratch_bytes,
+                       uint32_t K, int parts, int trans, void* scratch, size_t scratch_bytes,
                        cudaStream_t stream, uint32_t spin_limit, unsigned int* err);
+// row-major rows x cols -> cols x rows, elements of 4 or 8 bytes (adjoint.cu)
+int transpose_launch(const void* src, void* dst, uint64_t rows, uint64_t cols, size_t elem,
+                     cudaStream_t stream);
 size_t allpairs_tc_scratch_bytes(uint32_t M, uint32_t N, uint32_t K, int parts);
 bool allpairs_tc_supported(uint32_t M, uint32_t N, uint32_t K, const void* A, const void* B,
                            const void* P);
@@ -179,7 +182,8 @@ extern "C" int scl_launch_map(scl_program* p, const scl_shape* sh, void* const* 
                               const void* extra, size_t extra_bytes, const scl_tuning* tu) {
   if (int st = check_prog(p, {SCL_KIND_MAP, SCL_KIND_MAP_VOID, SCL_KIND_MAP_INDEX,
                               SCL_KIND_MAP_INDEX_VOID, SCL_KIND_MAP_POINT,
-                              SCL_KIND_MAP_POINT_VOID, SCL_KIND_ZIP, SCL_KIND_ZIP_VOID}))
+                              SCL_KIND_MAP_POINT_VOID, SCL_KIND_ZIP, SCL_KIND_ZIP_VOID,
+                              SCL_KIND_MAP_ADJOINT, SCL_KIND_ZIP_ADJOINT}))
     return st;
   if (!sh) return fail(SCL_ERR_ARG, "null shape");
   const int kind = p->kind;
@@ -192,20 +196,34 @@ extern "C" int scl_launch_map(scl_program* p, const scl_shape* sh, void* const* 
     case SCL_KIND_MAP_POINT: nbuf = 1; break;
     case SCL_KIND_ZIP: nbuf = 3; break;
     case SCL_KIND_ZIP_VOID: nbuf = 2; break;
+    case SCL_KIND_MAP_ADJOINT: nbuf = 3; break;  // x, g, gx
+    case SCL_KIND_ZIP_ADJOINT: nbuf = 5; break;  // x, y, g, gx, gy
     default: nbuf = 0;
   }
   if (nbuf && !bufs) return fail(SCL_ERR_ARG, "null buffer list");
-  void* b[3] = {nullptr, nullptr, nullptr};
+  void* b[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   for (int i = 0; i < nbuf; ++i) {
     b[i] = bufs[i];
-    if (!b[i]) return fail(SCL_ERR_ARG, "null device buffer " + std::to_string(i));
+    // the Zip adjoint may skip one of its two gradients
+    const bool optional = kind == SCL_KIND_ZIP_ADJOINT && i >= 3;
+    if (!b[i] && !optional) return fail(SCL_ERR_ARG, "null device buffer " + std::to_string(i));
   }
+  int acc = 0;
+  if (kind == SCL_KIND_ZIP_ADJOINT) {
+    if (!b[3] && !b[4]) return fail(SCL_ERR_ARG, "Zip adjoint: both gradient buffers are null");
+    if (b[4] && p->source.find("#define SCL_HAS_FUNC2") == std::string::npos)
+      return fail(SCL_ERR_ARG, "Zip adjoint: a right gradient needs the right derivative (func2)");
+    acc = ((sh->flags & SCL_SHAPE_ACCUMULATE) ? 1 : 0) | ((sh->flags & SCL_SHAPE_ACCUMULATE_RIGHT) ? 2 : 0);
+  } else if (kind == SCL_KIND_MAP_ADJOINT) {
+    acc = (sh->flags & SCL_SHAPE_ACCUMULATE) ? 1 : 0;
+  }
+  const bool adjoint = kind == SCL_KIND_MAP_ADJOINT || kind == SCL_KIND_ZIP_ADJOINT;
   uint64_t n = sh->n, rows = sh->rows, cols = sh->cols, offset = sh->offset;
   if (point) n = rows * cols;
   if (n == 0) return SCL_OK;
   bool simple = p->uses_workitem || (tu && tu->variant == SCL_VARIANT_SIMPLE);
   int aligned = 1;
-  for (int i = 0; i < nbuf; ++i) aligned &= aligned16(b[i]) ? 1 : 0;
+  for (int i = 0; i < nbuf; ++i) aligned &= (!b[i] || aligned16(b[i])) ? 1 : 0;
   uint32_t items = (tu && tu->items) ? tu->items : 4;
   if (items != 1 && items != 2 && items != 4) items = 4;
   std::string kname = simple ? "scl_map_simple" : "scl_map_k<" + std::to_string(items) + ">";
@@ -222,6 +240,7 @@ extern "C" int scl_launch_map(scl_program* p, const scl_shape* sh, void* const* 
   } else {
     pack.ptrs.push_back(&n);
     if (kind == SCL_KIND_MAP_INDEX || kind == SCL_KIND_MAP_INDEX_VOID) pack.ptrs.push_back(&offset);
+    if (adjoint) pack.ptrs.push_back(&acc);
   }
   if (!simple) pack.ptrs.push_back(&aligned);
   const size_t fixed = pack.ptrs.size();
@@ -459,6 +478,8 @@ extern "C" int scl_launch_allpairs(scl_program* p, const scl_shape* sh, void* co
   unsigned int M = (unsigned int)sh->rows, N = (unsigned int)sh->cols, K = (unsigned int)sh->dim;
   if (M == 0 || N == 0) return SCL_OK;
   if (K == 0) return fail(SCL_ERR_ARG, "AllPairs inner dimension is 0");
+  const int trans = ((sh->flags & SCL_SHAPE_TRANS_LEFT) ? 1 : 0) |
+                    ((sh->flags & SCL_SHAPE_TRANS_RIGHT) ? 2 : 0);
   if (p->kind == SCL_KIND_ALLPAIRS) {
     const uint32_t want = tu ? tu->variant : SCL_VARIANT_AUTO;
     if (p->tc_eligible && want != SCL_VARIANT_SIMT && extra_bytes == 0 &&
@@ -468,7 +489,7 @@ extern "C" int scl_launch_allpairs(scl_program* p, const scl_shape* sh, void* co
       const size_t need = allpairs_tc_scratch_bytes(M, N, K, parts);
       if (int st = ensure_workspace(p, need)) return st;
       p->last_variant = SCL_VARIANT_TC3XBF16;
-      return allpairs_tc_launch((const float*)A, (const float*)B, (float*)P, M, N, K, parts,
+      return allpairs_tc_launch((const float*)A, (const float*)B, (float*)P, M, N, K, parts, trans,
                                 p->ws.ptr, p->ws.bytes, rt().stream, spin_of(tu), rt().dev_err);
     }
     if (want == SCL_VARIANT_TC3XBF16)
@@ -476,6 +497,23 @@ extern "C" int scl_launch_allpairs(scl_program* p, const scl_shape* sh, void* co
                                        "float operands, no extra arguments and supported shapes");
     CUfunction fn = find_kernel(p, "scl_allpairs_simt");
     if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_allpairs_simt missing");
+    if (trans) {
+      // CUDA-core kernel: transposed operands are first stored row-major in
+      // the program's workspace
+      const size_t s0 = p->type_sizes[0], s1 = p->type_sizes[1];
+      const size_t a_bytes = (trans & 1) ? ((size_t)M * K * s0 + 255) / 256 * 256 : 0;
+      const size_t b_bytes = (trans & 2) ? (size_t)K * N * s1 : 0;
+      if (int st = ensure_workspace(p, a_bytes + b_bytes)) return st;
+      char* ws = static_cast<char*>(p->ws.ptr);
+      if (trans & 1) {
+        if (int st = transpose_launch(A, ws, K, M, s0, rt().stream)) return st;
+        A = ws;
+      }
+      if (trans & 2) {
+        if (int st = transpose_launch(B, ws + a_bytes, N, K, s1, rt().stream)) return st;
+        B = ws + a_bytes;
+      }
+    }
     int vec_a = (p->type_sizes[0] == 4 && K % 4 == 0 && aligned16(A)) ? 1 : 0;
     int vec_b = (p->type_sizes[1] == 4 && N % 4 == 0 && aligned16(B)) ? 1 : 0;
     ArgPack pack;
@@ -487,6 +525,7 @@ extern "C" int scl_launch_allpairs(scl_program* p, const scl_shape* sh, void* co
     p->last_variant = SCL_VARIANT_SIMT;
     return launch(fn, grid, dim3(256), 0, pack);
   }
+  if (trans) return fail(SCL_ERR_UNSUPPORTED, "transposed operands: only the Reduce/Zip AllPairs");
   CUfunction fn = find_kernel(p, "scl_allpairs_generic");
   if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_allpairs_generic missing");
   const size_t s0 = p->type_sizes[0], s1 = p->type_sizes[1];

@@ -78,6 +78,10 @@ int skeleton_arity(int kind) {
       return 2;
     case SCL_KIND_ALLPAIRS_GENERIC:
       return 3;
+    case SCL_KIND_MAP_ADJOINT:
+      return 2;  // x, g
+    case SCL_KIND_ZIP_ADJOINT:
+      return 3;  // x, y, g
     case SCL_KIND_ALLPAIRS:
       return 2;  // both the Reduce and the Zip take two
     default:
@@ -223,7 +227,23 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
     // Stencil taps: unrolled loops let the compiler read each staged input and
     // each weight once per thread across the rows it computes.
     if (kind == SCL_KIND_MAPOVERLAP) renamed = unroll_loops_in(renamed, target);
+    std::string second;  // Zip adjoint: the right operand's derivative
+    if (kind == SCL_KIND_ZIP_ADJOINT && d->func2 && *d->func2) {
+      const std::string func2 = d->func2;
+      const bool own = d->source2 && *d->source2;
+      const std::string src2 = own ? strip_opencl_pragmas(d->source2) : renamed;
+      FuncSig sig2;
+      if (!parse_function(src2, func2, &sig2, err)) { *err = "right derivative: " + *err; return SCL_ERR_COMPILE; }
+      if (sig2.params.size() != sig.params.size()) {
+        *err = "the two derivative functions must take the same parameters (x, y, g, extra...)";
+        return SCL_ERR_COMPILE;
+      }
+      if (own) second = rename_identifier(src2, func2, "SCL_FUNC2");
+      else renamed = rename_identifier(renamed, func2, "SCL_FUNC2");
+      s << "#define SCL_HAS_FUNC2 1\n";
+    }
     s << "// ---- user source\n" << renamed << "\n";
+    if (!second.empty()) s << "// ---- right derivative source\n" << second << "\n";
     p->uses_workitem = source_uses_workitem(src);
     if (want_f64) {
       // FP64 twin of the user function for cross-block carries
@@ -254,6 +274,7 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
     case SCL_KIND_MAP: case SCL_KIND_MAP_VOID: case SCL_KIND_MAP_INDEX:
     case SCL_KIND_MAP_INDEX_VOID: case SCL_KIND_MAP_POINT: case SCL_KIND_MAP_POINT_VOID:
     case SCL_KIND_ZIP: case SCL_KIND_ZIP_VOID:
+    case SCL_KIND_MAP_ADJOINT: case SCL_KIND_ZIP_ADJOINT:
       s << scl_tpl_elementwise;
       out->kernels = {"scl_map_k<1>", "scl_map_k<2>", "scl_map_k<4>", "scl_map_simple"};
       break;

@@ -239,3 +239,145 @@ extern "C" __global__ void scl_map_simple(const SCL_TYPE_0* left, const SCL_TYPE
   if (i < n) SCL_FUNC(left[i], right[i] SCL_EXTRA_ARGS);
 }
 #endif
+
+// ---------------------------------------------------------------------------
+// Adjoints of Map and Zip (no counterpart in the reference).  The user gives
+// the vector-Jacobian product as source:
+//   Map<Tout(Tin)>:     Tin  d (Tin x, Tout g, extra...)          -> SCL_FUNC
+//   Zip<Tout(Tl,Tr)>:   Tl   dl(Tl x, Tr y, Tout g, extra...)     -> SCL_FUNC
+//                       Tr   dr(Tl x, Tr y, Tout g, extra...)     -> SCL_FUNC2
+// and the kernels write gx[i] = d(x[i], g[i]) or, with `acc` set, add it to
+// gx[i] (bit 0: gx, bit 1: gy).  A null gx / gy is skipped.
+// ---------------------------------------------------------------------------
+#if SCL_KIND == 14  // ------------------------ adjoint of Map<Tout(Tin)>
+template <int U>
+__global__ void scl_map_k(const SCL_TYPE_0* x, const SCL_TYPE_1* g, SCL_TYPE_0* gx, scl_u64 n,
+                          int acc, int aligned SCL_EXTRA_PARAMS) {
+  SCL_EXTRA_SETUP
+  constexpr int V = scl_vec_width<sizeof(SCL_TYPE_0), sizeof(SCL_TYPE_1)>::value;
+  const scl_u64 tid = SCL_TID(), nth = SCL_NTH();
+  const scl_u64 nvec = aligned ? n / V : 0;
+  for (scl_u64 j = tid; j < nvec; j += nth * U) {
+    scl_pack<SCL_TYPE_0, V> a[U], o[U];
+    scl_pack<SCL_TYPE_1, V> b[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const scl_u64 k = j + (scl_u64)u * nth;
+      if (k < nvec) {
+        a[u] = scl_load<SCL_TYPE_0, V>(x + k * V);
+        b[u] = scl_load<SCL_TYPE_1, V>(g + k * V);
+        if (acc) o[u] = scl_load<SCL_TYPE_0, V>(gx + k * V);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const scl_u64 k = j + (scl_u64)u * nth;
+      if (k < nvec) {
+        scl_pack<SCL_TYPE_0, V> r;
+#pragma unroll
+        for (int e = 0; e < V; ++e) {
+          r.v[e] = SCL_FUNC(a[u].v[e], b[u].v[e] SCL_EXTRA_ARGS);
+          if (acc) r.v[e] = o[u].v[e] + r.v[e];
+        }
+        scl_store<SCL_TYPE_0, V>(gx + k * V, r);
+      }
+    }
+  }
+  for (scl_u64 i = nvec * V + tid; i < n; i += nth) {
+    SCL_TYPE_0 r = SCL_FUNC(x[i], g[i] SCL_EXTRA_ARGS);
+    gx[i] = acc ? gx[i] + r : r;
+  }
+}
+extern "C" __global__ void scl_map_simple(const SCL_TYPE_0* x, const SCL_TYPE_1* g,
+                                          SCL_TYPE_0* gx, scl_u64 n, int acc SCL_EXTRA_PARAMS) {
+  SCL_EXTRA_SETUP
+  const size_t i = get_global_id(0);
+  if (i < n) {
+    SCL_TYPE_0 r = SCL_FUNC(x[i], g[i] SCL_EXTRA_ARGS);
+    gx[i] = acc ? gx[i] + r : r;
+  }
+}
+
+#elif SCL_KIND == 15  // ----------------------- adjoint of Zip<Tout(Tl,Tr)>
+#ifndef SCL_HAS_FUNC2
+#define SCL_FUNC2(...) SCL_TYPE_1()
+#endif
+template <int U>
+__global__ void scl_map_k(const SCL_TYPE_0* x, const SCL_TYPE_1* y, const SCL_TYPE_2* g,
+                          SCL_TYPE_0* gx, SCL_TYPE_1* gy, scl_u64 n, int acc,
+                          int aligned SCL_EXTRA_PARAMS) {
+  SCL_EXTRA_SETUP
+  constexpr int V = scl_vec_width<sizeof(SCL_TYPE_0), sizeof(SCL_TYPE_1),
+                                  sizeof(SCL_TYPE_2)>::value;
+  const scl_u64 tid = SCL_TID(), nth = SCL_NTH();
+  const scl_u64 nvec = aligned ? n / V : 0;
+  const bool wx = gx != nullptr, wy = gy != nullptr;
+  const bool ax = wx && (acc & 1), ay = wy && (acc & 2);
+  for (scl_u64 j = tid; j < nvec; j += nth * U) {
+    scl_pack<SCL_TYPE_0, V> a[U], ox[U];
+    scl_pack<SCL_TYPE_1, V> b[U], oy[U];
+    scl_pack<SCL_TYPE_2, V> c[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const scl_u64 k = j + (scl_u64)u * nth;
+      if (k < nvec) {
+        a[u] = scl_load<SCL_TYPE_0, V>(x + k * V);
+        b[u] = scl_load<SCL_TYPE_1, V>(y + k * V);
+        c[u] = scl_load<SCL_TYPE_2, V>(g + k * V);
+        if (ax) ox[u] = scl_load<SCL_TYPE_0, V>(gx + k * V);
+        if (ay) oy[u] = scl_load<SCL_TYPE_1, V>(gy + k * V);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const scl_u64 k = j + (scl_u64)u * nth;
+      if (k < nvec) {
+        if (wx) {
+          scl_pack<SCL_TYPE_0, V> r;
+#pragma unroll
+          for (int e = 0; e < V; ++e) {
+            r.v[e] = SCL_FUNC(a[u].v[e], b[u].v[e], c[u].v[e] SCL_EXTRA_ARGS);
+            if (ax) r.v[e] = ox[u].v[e] + r.v[e];
+          }
+          scl_store<SCL_TYPE_0, V>(gx + k * V, r);
+        }
+        if (wy) {
+          scl_pack<SCL_TYPE_1, V> r;
+#pragma unroll
+          for (int e = 0; e < V; ++e) {
+            r.v[e] = SCL_FUNC2(a[u].v[e], b[u].v[e], c[u].v[e] SCL_EXTRA_ARGS);
+            if (ay) r.v[e] = oy[u].v[e] + r.v[e];
+          }
+          scl_store<SCL_TYPE_1, V>(gy + k * V, r);
+        }
+      }
+    }
+  }
+  for (scl_u64 i = nvec * V + tid; i < n; i += nth) {
+    if (wx) {
+      SCL_TYPE_0 r = SCL_FUNC(x[i], y[i], g[i] SCL_EXTRA_ARGS);
+      gx[i] = ax ? gx[i] + r : r;
+    }
+    if (wy) {
+      SCL_TYPE_1 r = SCL_FUNC2(x[i], y[i], g[i] SCL_EXTRA_ARGS);
+      gy[i] = ay ? gy[i] + r : r;
+    }
+  }
+}
+extern "C" __global__ void scl_map_simple(const SCL_TYPE_0* x, const SCL_TYPE_1* y,
+                                          const SCL_TYPE_2* g, SCL_TYPE_0* gx, SCL_TYPE_1* gy,
+                                          scl_u64 n, int acc SCL_EXTRA_PARAMS) {
+  SCL_EXTRA_SETUP
+  const size_t i = get_global_id(0);
+  if (i < n) {
+    if (gx) {
+      SCL_TYPE_0 r = SCL_FUNC(x[i], y[i], g[i] SCL_EXTRA_ARGS);
+      gx[i] = (acc & 1) ? gx[i] + r : r;
+    }
+    if (gy) {
+      SCL_TYPE_1 r = SCL_FUNC2(x[i], y[i], g[i] SCL_EXTRA_ARGS);
+      gy[i] = (acc & 2) ? gy[i] + r : r;
+    }
+  }
+}
+#endif

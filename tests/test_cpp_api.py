@@ -17,10 +17,10 @@ HOT_PATH_SUITES = ["MapTests", "ZipTests", "ReduceTests", "ScanTests", "MapOverl
                    "VectorTests", "MatrixTests", "DistributionTests"]
 
 
-def build_port(out: Path) -> None:
+def build_port(out: Path, source: str = "skelcl_api_tests.cpp") -> None:
     lib = ROOT / "skelcl_gb300"
     cmd = [CXX, "-std=c++17", "-O1", f"-I{ROOT / 'include'}", f"-I{ROOT / 'tests' / 'cpp'}",
-           str(ROOT / "tests" / "cpp" / "skelcl_api_tests.cpp"), f"-L{lib}", "-lskelcl_cuda",
+           str(ROOT / "tests" / "cpp" / source), f"-L{lib}", "-lskelcl_cuda",
            f"-Wl,-rpath,{lib}", "-o", str(out)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
@@ -43,6 +43,23 @@ def test_api_port_builds(built, tmp_path):
 def test_api_port_passes_on_gpu(built, tmp_path):
     exe = tmp_path / "skelcl_api_tests"
     build_port(exe)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=900,
+                       cwd=str(tmp_path), env=dict(os.environ))
+    tail = r.stdout[-6000:] + r.stderr[-2000:]
+    assert r.returncode == 0, tail
+    assert " 0 failed." in r.stdout, tail
+
+
+def test_adjoint_tape_builds(built, tmp_path):
+    build_port(tmp_path / "adjoint_tests", "adjoint_tests.cpp")
+
+
+@pytest.mark.gpu
+def test_adjoint_tape_passes_on_gpu(built, tmp_path):
+    """The reverse-mode tape (include/SkelCL/Adjoint.h): gradients against FP64
+    finite differences and against gradients composed from forward skeletons."""
+    exe = tmp_path / "adjoint_tests"
+    build_port(exe, "adjoint_tests.cpp")
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=900,
                        cwd=str(tmp_path), env=dict(os.environ))
     tail = r.stdout[-6000:] + r.stderr[-2000:]
