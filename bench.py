@@ -315,6 +315,37 @@ def secondary(S, oracle, hbm_peak, args):
         "note": "inputs 128 MiB, about L2 size: figures include L2 reuse across iterations"}
     del da, db, dz, dr
 
+    # Map / Zip / Reduce at 2^26 and their adjoints (the user's vector-Jacobian
+    # products; the broadcast for Reduce(+))
+    n = 1 << 26
+    xa = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 2, -1.0, 1.0))
+    ya = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 4, -1.0, 1.0))
+    ga = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 3, -1.0, 1.0))
+    o1, o2 = S.DeviceArray(n, np.float32), S.DeviceArray(n, np.float32)
+    mp = S.Program(S.KIND_MAP, "float func(float x){ return x*x + 1.0f; }", ["float", "float"])
+    mpa = S.Program(S.KIND_MAP_ADJOINT, "float d(float x, float g){ return 2.0f*x*g; }", ["float", "float"], func="d")
+    zpf = S.Program(S.KIND_ZIP, "float func(float x, float y){ return x*y; }", ["float"] * 3)
+    zpa = S.Program(S.KIND_ZIP_ADJOINT, "float dl(float x, float y, float g){ return y*g; }\n"
+                    "float dr(float x, float y, float g){ return x*g; }", ["float"] * 3, func="dl", func2="dr")
+    rpf = S.Program(S.KIND_REDUCE, "float func(float x, float y){ return x+y; }", ["float"], identity="0")
+    L = S.lib()
+    adj = {}
+    for name, f_bytes, a_bytes, fwd_fn, adj_fn in (
+            ("map_x*x+1", 8, 12, lambda: mp.launch([xa, o1], n=n), lambda: mpa.launch([xa, ga, o1], n=n)),
+            ("zip_x*y", 12, 20, lambda: zpf.launch([xa, ya, o1], n=n),
+             lambda: zpa.launch([xa, ya, ga, o1, o2], n=n)),
+            ("reduce_sum", 4, 4, lambda: rpf.launch([xa, o2], n=n),
+             lambda: S.check(L.scl_adjoint_broadcast(ga.ptr, o1.ptr, n, S.DTYPE_F32, 0)))):
+        f_ms = timed(S, fwd_fn, 10, 3)
+        a_ms = timed(S, adj_fn, 10, 3)
+        adj[name] = {"fwd_GBps": round(f_bytes * n / f_ms / 1e6, 1),
+                     "adjoint_GBps": round(a_bytes * n / a_ms / 1e6, 1),
+                     "adjoint_frac": round(a_bytes * n / a_ms / 1e6 / hbm_peak, 3),
+                     "fwd_plus_adjoint_over_fwd": round((f_ms + a_ms) / f_ms, 3),
+                     "bytes_per_elem_fwd_adjoint": [f_bytes, a_bytes]}
+    out["elementwise_adjoints_2^26"] = adj
+    del xa, ya, ga, o1, o2
+
     # float scan 2^26 and its adjoint (reverse scan of the upstream gradient)
     n = 1 << 26
     xf = oracle.uniform_f32(n, 2, -1.0, 1.0)
@@ -342,17 +373,34 @@ def secondary(S, oracle, hbm_peak, args):
            " for (int dy = -5; dy <= 5; ++dy) for (int dx = -5; dx <= 5; ++dx)"
            "  s += getData(img, dx, dy) * w[(dy + 5) * 11 + (dx + 5)]; return s; }")
     di, do, dw = S.DeviceArray.from_numpy(img), S.DeviceArray(rows * cols, np.float32), S.DeviceArray.from_numpy(w.ravel())
+    # adjoint of the linear stencil: the zero-padded transposed stencil (flipped
+    # weights), plus the edge fold for NEAREST
+    dwt = S.DeviceArray.from_numpy(np.ascontiguousarray(w.reshape(11, 11)[::-1, ::-1]).ravel())
+    dg = S.DeviceArray.from_numpy(oracle.uniform_f32(rows * cols, 6, -1.0, 1.0))
+    adj_src = ("float adj(input_matrix_t g, __global const float* w) { float s = 0.0f;"
+               " for (int dy = -5; dy <= 5; ++dy) for (int dx = -5; dx <= 5; ++dx)"
+               "  s += w[(dy + 5) * 11 + (dx + 5)] * getData(g, dx, dy); return s; }")
+    pa = S.Program(S.KIND_MAPOVERLAP, adj_src, ["float", "float"], func="adj", overlap_range=5,
+                   padding=S.PAD_NEUTRAL, neutral="0.0f")
     mo = {}
     for name, pad in (("neutral", S.PAD_NEUTRAL), ("nearest", S.PAD_NEAREST)):
         p = S.Program(S.KIND_MAPOVERLAP, src, ["float", "float"], overlap_range=5, padding=pad, neutral="0")
         ms = timed(S, lambda: p.launch([di, do], rows=rows, cols=cols, extra=S.buffer(dw)), 10, 3)
         gbps = 8 * rows * cols / ms / 1e6
         tflops = 242 * rows * cols / ms / 1e9
+
+        def adjoint():
+            pa.launch([dg, do], rows=rows, cols=cols, extra=S.buffer(dwt))
+            if pad == S.PAD_NEAREST:
+                S.check(L.scl_mapoverlap_adjoint_edges(dg.ptr, dwt.ptr, do.ptr, rows, cols, 5))
+
+        a_ms = timed(S, adjoint, 10, 3)
         mo[name] = {"GBps": round(gbps, 1), "hbm_frac": round(gbps / hbm_peak, 3),
                     "TFLOPs": round(tflops, 2), "fp32_frac_nominal": round(tflops / fp32_peak, 3),
-                    "variant": p.last_variant}
+                    "variant": p.last_variant, "adjoint_ms": round(a_ms, 4), "fwd_ms": round(ms, 4),
+                    "fwd_plus_adjoint_over_fwd": round((ms + a_ms) / ms, 3)}
     out["mapoverlap_8192^2_R5"] = mo
-    del di, do, dw
+    del di, do, dw, dwt, dg
 
     # AllPairs 8192x4096 . 4096x8192 (mult/add), and Manhattan 4096x256 . 256x4096
     M, K, N = 8192, 4096, 8192
@@ -376,8 +424,17 @@ def secondary(S, oracle, hbm_peak, args):
                      "median_rel_err_vs_fp64": float(np.median(err / np.maximum(np.abs(ref), 1e-30)))}
     res["speedup_tc6_over_simt"] = round(res["fp32_simt"]["ms"] / res["tc_3xbf16_6prod"]["ms"], 2)
     res["speedup_tc3_over_simt"] = round(res["fp32_simt"]["ms"] / res["tc_3xbf16_3prod"]["ms"], 2)
+    # backward of L = sum(G * P) as two AllPairs on transposed operands (tensor cores)
+    dG = S.DeviceArray.from_numpy(oracle.normal_f32(M * N, 9))
+    dgA, dgB = S.DeviceArray(M * K, np.float32), S.DeviceArray(K * N, np.float32)
+    f_ms = timed(S, lambda: ap.launch([dA, dB, dP], rows=M, cols=N, dim=K), 3, 1)
+    a_ms = timed(S, lambda: ap.launch([dG, dB, dgA], rows=M, cols=K, dim=N, flags=S.SHAPE_TRANS_RIGHT), 3, 1)
+    b_ms = timed(S, lambda: ap.launch([dA, dG, dgB], rows=K, cols=N, dim=M, flags=S.SHAPE_TRANS_LEFT), 3, 1)
+    res["backward_tc_3xbf16_6prod"] = {"fwd_ms": round(f_ms, 3), "dA_ms": round(a_ms, 3), "dB_ms": round(b_ms, 3),
+                                       "fwd_plus_adjoint_over_fwd": round((f_ms + a_ms + b_ms) / f_ms, 3),
+                                       "note": "two contractions of the forward's size: 3x is the flop bound"}
     out["allpairs_8192x4096x8192"] = res
-    del dA, dB, dP, A, B
+    del dA, dB, dP, A, B, dG, dgA, dgB
     Ml, Kl, Nl = 4096, 256, 4096
     L_ = oracle.normal_f32(Ml * Kl, 10)
     R_ = oracle.normal_f32(Kl * Nl, 11)

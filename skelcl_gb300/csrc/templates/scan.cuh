@@ -294,4 +294,211 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
       }
   }
 }
+
+// ---------------------------------------------------------------------------
+// Shared-memory staged variant.  One elected thread brings the tile into
+// shared memory with bulk asynchronous copies (completion counted on an
+// mbarrier), threads scan it there, and only the R warp totals per thread stay
+// in registers while warp 0 looks back: about 40 registers per thread, so the
+// SM holds as many tiles as its shared memory allows (6 of 32 KB) instead of
+// as many as the register file allows with the tile in registers (4).
+// Reverse, ragged and unaligned tiles are staged with ordinary loads.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool scl_mbar_wait(unsigned int bar_s, unsigned int spin_limit) {
+  unsigned int done = 0, polls = 0;
+  while (!done) {
+    asm volatile(
+        "{ .reg .pred p; mbarrier.test_wait.parity.shared::cta.b64 p, [%1], 0;"
+        " selp.u32 %0, 1, 0, p; }"
+        : "=r"(done) : "r"(bar_s) : "memory");
+    if (!done) {
+      if (++polls > spin_limit) return false;
+      if (polls > 16) scl_nanosleep(32);
+    }
+  }
+  return true;
+}
+
+template <int R, int MINB>
+__global__ void __launch_bounds__(SCL_SCAN_B, MINB)
+scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int aligned,
+           unsigned int* tile_counter, scl_scan_status st, unsigned int spin_limit,
+           unsigned int* err SCL_EXTRA_PARAMS) {
+  SCL_EXTRA_SETUP
+  constexpr int B = SCL_SCAN_B, W = SCL_SCAN_W;
+  constexpr int V = scl_vec_width<sizeof(scl_T)>::value;
+  constexpr int TILE = R * B * V;
+  constexpr unsigned int ROW_BYTES = B * V * sizeof(scl_T);
+  const bool inclusive = (flags & 1u) != 0, reverse = (flags & 2u) != 0;
+  const scl_T ident = (scl_T)(SCL_IDENTITY);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  scl_T* ts = reinterpret_cast<scl_T*>(scl_dyn_smem);  // the tile, logical order
+
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ unsigned int s_tile;
+  __shared__ int s_ok;
+  __shared__ scl_T s_wsum[R * W];
+  __shared__ scl_C s_prefix;
+  const unsigned int bar_s = (unsigned int)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) {
+    s_tile = atomicAdd(tile_counter, 1u);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar_s));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const unsigned int tile = s_tile;
+  const scl_u64 base = (scl_u64)tile * TILE;
+
+  // ---- stage the tile.  Full aligned tiles arrive by bulk copy in physical
+  //      order: for a reverse scan the slot of logical vector q is then
+  //      TILE - (q+1)*V with its elements reversed; the in-thread pass below
+  //      rewrites every slot in logical order.
+  const bool bulk = aligned && base + TILE <= n && (!reverse || n % V == 0);
+  const bool rev_slots = bulk && reverse;
+  if (bulk) {
+    const scl_T* src = reverse ? in + (n - base - TILE) : in + base;
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                   :: "r"(bar_s), "r"((unsigned int)(TILE * sizeof(scl_T))) : "memory");
+      const unsigned int dst = (unsigned int)__cvta_generic_to_shared(ts);
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+            :: "r"(dst + r * ROW_BYTES), "l"(src + (scl_u64)r * B * V), "r"(ROW_BYTES), "r"(bar_s)
+            : "memory");
+      const bool ok = scl_mbar_wait(bar_s, spin_limit);
+      if (!ok) {
+        scl_raise(err, SCL_DEV_ERR_TIMEOUT);
+        // The copies may still land in this block's shared memory: the block
+        // stays until they have (bounded by about 0.1 s, whatever the
+        // caller's poll limit), and the tile is not used.
+        scl_mbar_wait(bar_s, 1u << 21);
+      }
+      s_ok = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_ok) return;  // successors time out too and see the error flag
+  } else {
+    for (int k = threadIdx.x; k < TILE; k += B) {
+      const scl_u64 i = base + k;
+      ts[k] = i < n ? in[reverse ? n - 1 - i : i] : ident;
+    }
+    __syncthreads();
+  }
+
+  // ---- in-thread inclusive scan of each vector (kept in shared memory),
+  //      warp scans of the vector totals
+  scl_T wincl[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int q = r * B + threadIdx.x;
+    scl_T* vp = ts + (rev_slots ? TILE - (q + 1) * V : q * V);
+    scl_pack<scl_T, V> p = scl_load<scl_T, V>(vp);
+    if (rev_slots) {
+#pragma unroll
+      for (int e = 0; e < V / 2; ++e) {
+        const scl_T t = p.v[e];
+        p.v[e] = p.v[V - 1 - e];
+        p.v[V - 1 - e] = t;
+      }
+    }
+#pragma unroll
+    for (int e = 1; e < V; ++e) p.v[e] = SCL_FUNC(p.v[e - 1], p.v[e] SCL_EXTRA_ARGS);
+    scl_store<scl_T, V>(vp, p);
+    wincl[r] = scl_warp_incl(p.v[V - 1] SCL_EXTRA_ARGS);
+    if (lane == 31) s_wsum[r * W + warp] = wincl[r];
+  }
+  __syncthreads();
+
+  // ---- warp 0: tile aggregate, publication and look-back (as scl_scan_k)
+  if (warp == 0) {
+    scl_T carry = ident;
+#pragma unroll
+    for (int c = 0; c < (R * W + 31) / 32; ++c) {
+      const int q = c * 32 + lane;
+      scl_T v = q < R * W ? s_wsum[q] : ident;
+      scl_T vi = scl_warp_incl(v SCL_EXTRA_ARGS);
+      scl_T ve = scl_shfl_up(vi, 1);
+      if (lane == 0) ve = ident;
+      if (q < R * W) s_wsum[q] = SCL_FUNC(carry, ve SCL_EXTRA_ARGS);
+      scl_T total = scl_shfl_idx(vi, 31);
+      carry = SCL_FUNC(carry, total SCL_EXTRA_ARGS);
+    }
+    const scl_C aggc = (scl_C)carry;
+    scl_C prefix = (scl_C)ident;
+    if (lane == 0) scl_publish(st, tile, tile == 0, aggc);
+    if (tile != 0) {
+      scl_C running = (scl_C)ident;
+      long long pred = (long long)tile - 1;
+      while (true) {
+        const long long idx = pred - lane;
+        scl_C v = (scl_C)ident;
+        int kind = 2;
+        if (idx >= 0) {
+          kind = scl_poll(st, idx, spin_limit, &v);
+          if (kind == 0) {
+            scl_raise(err, SCL_DEV_ERR_TIMEOUT);
+            v = (scl_C)ident;
+            kind = 2;
+          }
+        }
+        const unsigned int pmask = __ballot_sync(0xffffffffu, kind == 2);
+        const int first = pmask ? __ffs(pmask) - 1 : 31;
+        if (lane > first) v = (scl_C)ident;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          scl_C o = scl_shfl_down(v, off);
+          if (lane + off < 32) v = (scl_C)SCL_FUNC_C(o, v SCL_EXTRA_ARGS);
+        }
+        const scl_C window = scl_shfl_idx(v, 0);
+        running = (scl_C)SCL_FUNC_C(window, running SCL_EXTRA_ARGS);
+        if (pmask) break;
+        pred -= 32;
+      }
+      prefix = running;
+      if (lane == 0) scl_publish(st, tile, true, (scl_C)SCL_FUNC_C(prefix, aggc SCL_EXTRA_ARGS));
+    }
+    if (lane == 0) s_prefix = prefix;
+  }
+  __syncthreads();
+
+  // ---- outputs
+  const scl_T tile_carry = (scl_T)s_prefix;
+  const bool vec_out = aligned && base + TILE <= n && (!reverse || n % V == 0);
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const scl_u64 q = (scl_u64)r * B + threadIdx.x;
+    scl_pack<scl_T, V> p = scl_load<scl_T, V>(ts + (rev_slots ? TILE - (q + 1) * V : q * V));
+    scl_T lane_excl = scl_shfl_up(wincl[r], 1);
+    if (lane == 0) lane_excl = ident;
+    const scl_T pre = SCL_FUNC(SCL_FUNC(tile_carry, s_wsum[r * W + warp] SCL_EXTRA_ARGS),
+                               lane_excl SCL_EXTRA_ARGS);
+    scl_pack<scl_T, V> o;
+    if (inclusive) {
+#pragma unroll
+      for (int e = 0; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e] SCL_EXTRA_ARGS);
+    } else {
+      o.v[0] = pre;
+#pragma unroll
+      for (int e = 1; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e - 1] SCL_EXTRA_ARGS);
+    }
+    if (vec_out) {
+      if (!reverse) {
+        scl_store<scl_T, V>(out + base + q * V, o);
+      } else {
+        scl_pack<scl_T, V> rv;
+#pragma unroll
+        for (int e = 0; e < V; ++e) rv.v[V - 1 - e] = o.v[e];
+        scl_store<scl_T, V>(out + (n - base - (q + 1) * V), rv);
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        const scl_u64 i = base + q * V + e;
+        if (i < n) out[reverse ? n - 1 - i : i] = o.v[e];
+      }
+    }
+  }
+}
 #endif
