@@ -100,7 +100,16 @@ typedef struct scl_shape {
   uint64_t dim;          /* AllPairs inner dimension                          */
   uint64_t offset;       /* Map<Index>: first index; Map<IndexPoint>: row offset */
   const uint64_t* seg_offsets; /* segmented launches: DEVICE array, n_segments+1 */
-  uint64_t n_segments;   /* 0 = not segmented                                 */
+  uint64_t n_segments;   /* 0 = not segmented.  Segment s = elements
+                            [seg_offsets[s], seg_offsets[s+1]) of the flat
+                            vector of n elements.  Scan: one scan per segment;
+                            Reduce: out gets n_segments results (SCL_IDENTITY
+                            for an empty segment); both in one launch after a
+                            small pre-pass.  Offsets must be non-decreasing and
+                            at most n (they are clamped, and the next
+                            scl_sync reports SCL_ERR_ARG).  Map/Zip are
+                            element-wise: segments do not change them.  No
+                            counterpart in the reference.                     */
   uint32_t flags;        /* SCL_SHAPE_* below                                 */
   uint32_t reserved;
 } scl_shape;
@@ -264,6 +273,11 @@ enum scl_dtype { SCL_DTYPE_F32 = 1, SCL_DTYPE_F64 = 2 };
 /* Adjoint of Reduce(+): gx[i] = g (or gx[i] += g with `accumulate`), g read
  * from DEVICE memory (the gradient of the reduced scalar). */
 int scl_adjoint_broadcast(const void* g, void* gx, uint64_t n, int dtype, int accumulate);
+/* Adjoint of a segmented Reduce(+): gx[i] = g[s] (or += with `accumulate`)
+ * for every element i of segment s (shape.seg_offsets semantics, DEVICE
+ * offsets, n = length of gx). */
+int scl_adjoint_broadcast_segments(const void* g, void* gx, const uint64_t* seg_offsets,
+                                   uint64_t n_segments, uint64_t n, int dtype, int accumulate);
 /* dst[i] += src[i]: gradient accumulation where an adjoint cannot add itself. */
 int scl_adjoint_accumulate(void* dst, const void* src, uint64_t n, int dtype);
 /* Adjoint of a linear MapOverlap with NEAREST padding, edge part.  With

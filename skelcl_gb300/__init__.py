@@ -105,6 +105,7 @@ SIGNATURES = {
     "scl_debug_bounded_wait": ([_U32, ctypes.POINTER(_I)], _I),
     "scl_adjoint_broadcast": ([_VP, _VP, _U64, _I, _I], _I),
     "scl_adjoint_accumulate": ([_VP, _VP, _U64, _I], _I),
+    "scl_adjoint_broadcast_segments": ([_VP, _VP, _VP, _U64, _U64, _I, _I], _I),
     "scl_mapoverlap_adjoint_edges": ([_VP, _VP, _VP, _U64, _U64, _I], _I),
 }
 
@@ -192,7 +193,9 @@ class DeviceArray:
         return out
 
     def view(self, offset_elems: int, n: int) -> "DeviceArray":
-        return DeviceArray(n, self.dtype, ptr=self.ptr + offset_elems * self.dtype.itemsize)
+        v = DeviceArray(n, self.dtype, ptr=self.ptr + offset_elems * self.dtype.itemsize)
+        v._base = self  # the allocation lives as long as its views
+        return v
 
     def free(self) -> None:
         if self._owned and self.ptr:
@@ -312,11 +315,13 @@ class Program:
 
     def launch(self, bufs: Iterable, n: int = 0, rows: int = 0, cols: int = 0, dim: int = 0,
                offset: int = 0, flags: int = 0, extra: bytes = b"",
-               tuning: Optional[Tuning] = None) -> None:
+               tuning: Optional[Tuning] = None, segments: Optional["DeviceArray"] = None) -> None:
+        """`segments`: a DeviceArray of n_segments+1 uint64 offsets (segmented Scan/Reduce)."""
         ptrs = [b.ptr if isinstance(b, DeviceArray) else (b or 0) for b in bufs]
         arr = (ctypes.c_void_p * max(1, len(ptrs)))(*ptrs)
-        sh = Shape(n=n, rows=rows, cols=cols, dim=dim, offset=offset, seg_offsets=None,
-                   n_segments=0, flags=flags, reserved=0)
+        sh = Shape(n=n, rows=rows, cols=cols, dim=dim, offset=offset,
+                   seg_offsets=segments.ptr if segments is not None else None,
+                   n_segments=(segments.n - 1) if segments is not None else 0, flags=flags, reserved=0)
         eb = ctypes.create_string_buffer(extra, len(extra)) if extra else None
         fn = getattr(lib(), _LAUNCH[self.kind])
         check(fn(self.handle, ctypes.byref(sh), arr, eb, len(extra),

@@ -152,6 +152,14 @@ int pack_extra(scl_program* p, CUfunction fn, size_t fixed, const unsigned char*
                size_t bytes, ArgPack* pack);
 // cuLaunchKernel on the library stream.
 int launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, ArgPack& pack);
+
+// Device status word bits (bit 0: a bounded wait gave up, set by the
+// generated kernels).
+constexpr unsigned int kDevErrSegments = 2u;  // segment offsets decreasing or past the end
+// Pre-pass of segmented launches (segments.cu): sanitised offsets and the
+// first tile of every segment (tile_start[n_seg] = tile count).
+int segments_prepare(const uint64_t* seg_offsets, uint64_t n_seg, uint64_t n_total, uint64_t tile,
+                     uint64_t* off_out, unsigned int* tile_start, cudaStream_t stream);
 // Autotuner lookup/store; returns false when nothing is cached.
 bool tune_lookup(const std::string& key, scl_tuning* out);
 void tune_store(const std::string& key, const scl_tuning& t);

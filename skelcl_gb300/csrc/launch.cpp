@@ -309,6 +309,35 @@ extern "C" int scl_launch_reduce(scl_program* p, const scl_shape* sh, void* cons
   const size_t tsz = p->type_sizes[0], csz = p->carry_size ? p->carry_size : tsz;
   const int V = vec_width(tsz);
   int aligned = aligned16(in) ? 1 : 0;
+  if (sh->n_segments) {
+    // one result per segment, one launch (plus the offsets pre-pass)
+    if (!sh->seg_offsets) return fail(SCL_ERR_ARG, "segmented reduce: null seg_offsets");
+    uint64_t n_seg = sh->n_segments;
+    const uint64_t tile = 8ull * 256 * V;
+    const uint64_t tiles = (n + tile - 1) / tile + n_seg;
+    if (tiles > 0x7fffffffull) return fail(SCL_ERR_ARG, "segmented reduce: too many tiles");
+    CUfunction fn = find_kernel(p, "scl_reduce_seg<8>");
+    if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_reduce_seg<8> missing");
+    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t tk = up(n_seg * 4), pa = up(tiles * csz), of = up((n_seg + 1) * 8);
+    if (int st = ensure_workspace(p, tk + pa + of + up((n_seg + 1) * 4))) return st;
+    char* ws = static_cast<char*>(p->ws.ptr);
+    void* tickets = ws;
+    void* partials = ws + tk;
+    void* offs = ws + tk + pa;
+    void* tstart = ws + tk + pa + of;
+    SCL_CUDA(cudaMemsetAsync(tickets, 0, tk, rt().stream));
+    if (int st = segments_prepare(sh->seg_offsets, n_seg, n, tile, (uint64_t*)offs,
+                                  (unsigned int*)tstart, rt().stream))
+      return st;
+    unsigned int* err = rt().dev_err;
+    ArgPack pack;
+    pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err};
+    if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
+      return st;
+    p->last_variant = SCL_VARIANT_VECTOR;
+    return launch(fn, dim3((unsigned)tiles), dim3(256), 0, pack);
+  }
   uint32_t items = (tu && tu->items) ? tu->items : 4;
   if (items != 1 && items != 2 && items != 4) items = 4;
   std::string kname = "scl_reduce_k<" + std::to_string(items) + ">";
@@ -362,8 +391,17 @@ extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const*
     staged = false;
     smem = 0;
   }
+  uint64_t n_seg = sh->n_segments;
+  if (n_seg) {  // segmented: the staged kernel with the default tile shape
+    if (!sh->seg_offsets) return fail(SCL_ERR_ARG, "segmented scan: null seg_offsets");
+    staged = true;
+    R = 8;
+    smem = (size_t)R * 256 * V * tsz;
+    if (smem + 2048 > rt().smem_optin)
+      return fail(SCL_ERR_UNSUPPORTED, "segmented scan: the tile does not fit in shared memory");
+  }
   const uint64_t tile = (uint64_t)R * 256 * V;
-  const uint64_t tiles = (n + tile - 1) / tile;
+  const uint64_t tiles = (n + tile - 1) / tile + n_seg;  // segmented: an upper bound
   if (tiles > 0x7fffffffull) return fail(SCL_ERR_ARG, "scan input too large");
   // resident tiles per SM the register (or shared-memory) budget is sized for
   uint32_t minb = (tu && tu->tile_w) ? tu->tile_w : 0;
@@ -375,8 +413,9 @@ extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const*
                (R == 4 && (minb == 4 || minb == 6)) || (R == 2 && minb == 8))) {
     minb = R == 16 ? 2 : (R == 8 ? 4 : (R == 4 ? 6 : 8));
   }
+  if (n_seg) minb = 6;
   const std::string kname = std::string(staged ? "scl_scan_s<" : "scl_scan_k<") + std::to_string(R) +
-                            ", " + std::to_string(minb) + ">";
+                            ", " + std::to_string(minb) + (n_seg ? ", 1>" : ">");
   CUfunction fn = find_kernel(p, kname);
   if (!fn) return fail(SCL_ERR_LAUNCH, "kernel " + kname + " missing");
   // workspace: [tile counter | status words / flags | values], zeroed by one memset
@@ -387,27 +426,41 @@ extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const*
     void* agg;
     void* incl;
   } sargs = {nullptr, nullptr, nullptr, nullptr};
+  // segmented launches add [sanitised offsets | tile numbering] after the status
   size_t clear_bytes, total;
+  const size_t seg_of = n_seg ? up((n_seg + 1) * 8) : 0, seg_ts = n_seg ? up((n_seg + 1) * 4) : 0;
   if (p->status_mode != 0) {
     clear_bytes = 256 + up(tiles * 128);  // one 128-byte line per tile slot
     total = clear_bytes;
-    if (int st = ensure_workspace(p, total)) return st;
+    if (int st = ensure_workspace(p, total + seg_of + seg_ts)) return st;
     sargs.slots = (char*)p->ws.ptr + 256;
   } else {
     const size_t fl = up(tiles * 4), vals = up(tiles * csz);
     clear_bytes = 256 + fl;
     total = clear_bytes + 2 * vals;
-    if (int st = ensure_workspace(p, total)) return st;
+    if (int st = ensure_workspace(p, total + seg_of + seg_ts)) return st;
     sargs.flags = (char*)p->ws.ptr + 256;
     sargs.agg = (char*)p->ws.ptr + 256 + fl;
     sargs.incl = (char*)p->ws.ptr + 256 + fl + vals;
   }
   void* counter = p->ws.ptr;
+  void* seg_off = n_seg ? (char*)p->ws.ptr + total : nullptr;
+  void* tile_start = n_seg ? (char*)p->ws.ptr + total + seg_of : nullptr;
   SCL_CUDA(cudaMemsetAsync(p->ws.ptr, 0, clear_bytes, rt().stream));
+  if (n_seg) {
+    if (int st = segments_prepare(sh->seg_offsets, n_seg, n, tile, (uint64_t*)seg_off,
+                                  (unsigned int*)tile_start, rt().stream))
+      return st;
+  }
   unsigned int spin = spin_of(tu);
   unsigned int* err = rt().dev_err;
   ArgPack pack;
   pack.ptrs = {&in, &out, &n, &flags, &aligned, &counter, &sargs, &spin, &err};
+  if (staged) {
+    pack.ptrs.push_back(&seg_off);
+    pack.ptrs.push_back(&tile_start);
+    pack.ptrs.push_back(&n_seg);
+  }
   if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
     return st;
   p->last_variant = staged ? SCL_VARIANT_TMA : SCL_VARIANT_VECTOR;

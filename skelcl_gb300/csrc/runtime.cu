@@ -192,6 +192,8 @@ int check_device_status() {
   if (v) {
     SCL_CUDA(cudaMemset(g_rt.dev_err, 0, sizeof(unsigned int)));
     if (v & 1u) return fail(SCL_ERR_TIMEOUT, "a bounded device-side wait gave up (decoupled look-back or TMA barrier)");
+    if (v & kDevErrSegments)
+      return fail(SCL_ERR_ARG, "segment offsets were decreasing or beyond the vector (clamped)");
     return fail(SCL_ERR_CUDA, "device reported status " + std::to_string(v));
   }
   return SCL_OK;

@@ -193,4 +193,97 @@ __global__ void scl_reduce_k(const scl_T* in, scl_T* out, scl_u64 n, int aligned
     *ticket = 0u;  // ready for the next launch on this workspace
   }
 }
+
+// Segmented Reduce (no counterpart in the reference): out[s] = the fold of
+// segment [seg_off[s], seg_off[s+1]) of the flat vector, for every segment,
+// in one launch.  Tiles of R x 256 vectors never span segments (segment s
+// owns tiles tile_start[s] .. tile_start[s+1]-1, at least one); each tile
+// folds its elements into partials[tile], and the last tile of a segment to
+// finish (per-segment ticket, reset afterwards) folds that segment's
+// partials.  An empty segment yields SCL_IDENTITY.  Blocks past the last
+// tile (the grid is an upper bound) return at once.
+template <int R>
+__global__ void __launch_bounds__(256)
+scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
+               const unsigned int* tile_start, scl_u64 n_seg, int aligned, scl_C* partials,
+               unsigned int* tickets, unsigned int* err SCL_EXTRA_PARAMS) {
+  SCL_EXTRA_SETUP
+  constexpr int V = scl_vec_width<sizeof(scl_T)>::value;
+  constexpr int B = 256;
+  constexpr scl_u64 TILE = (scl_u64)R * B * V;
+  const unsigned int tile = blockIdx.x;
+  __shared__ long long s_seg;
+  if (threadIdx.x == 0) {
+    long long sg = -1;
+    if (tile < tile_start[n_seg]) {
+      scl_u64 lo = 0, hi = n_seg - 1;
+      while (lo < hi) {
+        const scl_u64 mid = (lo + hi + 1) / 2;
+        if (tile_start[mid] <= tile) lo = mid; else hi = mid - 1;
+      }
+      sg = (long long)lo;
+    }
+    s_seg = sg;
+  }
+  __syncthreads();
+  if (s_seg < 0) return;
+  const scl_u64 sg = (scl_u64)s_seg;
+  const unsigned int first = tile_start[sg], count = tile_start[sg + 1] - first;
+  const scl_u64 off = seg_off[sg], len = seg_off[sg + 1] - off;
+  if (len == 0) {
+    if (threadIdx.x == 0) out[sg] = (scl_T)(SCL_IDENTITY);
+    return;
+  }
+  const scl_T* src = in + off;
+  const scl_u64 begin = (scl_u64)(tile - first) * TILE;
+  const scl_u64 end = begin + TILE < len ? begin + TILE : len;
+  bool have = false;
+  scl_T acc;
+  const bool vec = aligned && ((off * sizeof(scl_T)) % 16 == 0) && end - begin == TILE;
+  if (vec) {
+    scl_pack<scl_T, V> a[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) a[r] = scl_load<scl_T, V>(src + begin + ((scl_u64)r * B + threadIdx.x) * V);
+    acc = a[0].v[0];
+#pragma unroll
+    for (int e = 1; e < V; ++e) acc = SCL_FUNC(acc, a[0].v[e] SCL_EXTRA_ARGS);
+#pragma unroll
+    for (int r = 1; r < R; ++r)
+#pragma unroll
+      for (int e = 0; e < V; ++e) acc = SCL_FUNC(acc, a[r].v[e] SCL_EXTRA_ARGS);
+    have = true;
+  } else {
+    for (scl_u64 i = begin + threadIdx.x; i < end; i += B) {
+      acc = have ? SCL_FUNC(acc, src[i] SCL_EXTRA_ARGS) : src[i];
+      have = true;
+    }
+  }
+  scl_C c;
+  if (have) c = (scl_C)acc;
+  scl_block_fold(have, c SCL_EXTRA_ARGS);
+  if (count == 1) {  // the segment's only tile
+    if (threadIdx.x == 0) out[sg] = (scl_T)c;
+    return;
+  }
+  __shared__ int s_last;
+  if (threadIdx.x == 0) {
+    scl_st_cg(&partials[tile], c);
+    __threadfence();
+    s_last = (atomicAdd(&tickets[sg], 1u) == count - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  have = false;
+  for (unsigned int b = threadIdx.x; b < count; b += B) {
+    scl_C v = scl_ld_cg(&partials[first + b]);
+    c = have ? (scl_C)SCL_FUNC_C(c, v SCL_EXTRA_ARGS) : v;
+    have = true;
+  }
+  scl_block_fold(have, c SCL_EXTRA_ARGS);
+  if (threadIdx.x == 0) {
+    out[sg] = (scl_T)c;
+    tickets[sg] = 0u;
+  }
+}
 #endif

@@ -319,11 +319,19 @@ __device__ __forceinline__ bool scl_mbar_wait(unsigned int bar_s, unsigned int s
   return true;
 }
 
-template <int R, int MINB>
+//
+// SEG = 1: a segmented scan, one independent scan per segment
+// [seg_off[s], seg_off[s+1]) of the flat vector.  Tiles never span segments:
+// segment s owns the tickets tile_start[s] .. tile_start[s+1]-1 (at least
+// one), a tile works on its segment with segment-relative pointers, and the
+// look-back stops at the segment's first tile.  Tickets past the last tile
+// (the grid is an upper bound) return at once.
+template <int R, int MINB, int SEG = 0>
 __global__ void __launch_bounds__(SCL_SCAN_B, MINB)
 scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int aligned,
            unsigned int* tile_counter, scl_scan_status st, unsigned int spin_limit,
-           unsigned int* err SCL_EXTRA_PARAMS) {
+           unsigned int* err, const scl_u64* seg_off, const unsigned int* tile_start,
+           scl_u64 n_seg SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
   constexpr int B = SCL_SCAN_B, W = SCL_SCAN_W;
   constexpr int V = scl_vec_width<sizeof(scl_T)>::value;
@@ -347,7 +355,35 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
   }
   __syncthreads();
   const unsigned int tile = s_tile;
-  const scl_u64 base = (scl_u64)tile * TILE;
+  unsigned int first = 0;  // ticket of the first tile of this tile's sequence
+  scl_u64 local = tile;    // tile index within the sequence
+  if constexpr (SEG != 0) {
+    __shared__ long long s_seg;
+    if (threadIdx.x == 0) {
+      long long sg = -1;
+      if (tile < tile_start[n_seg]) {
+        scl_u64 lo = 0, hi = n_seg - 1;  // largest s with tile_start[s] <= tile
+        while (lo < hi) {
+          const scl_u64 mid = (lo + hi + 1) / 2;
+          if (tile_start[mid] <= tile) lo = mid; else hi = mid - 1;
+        }
+        sg = (long long)lo;
+      }
+      s_seg = sg;
+    }
+    __syncthreads();
+    if (s_seg < 0) return;
+    const scl_u64 sg = (scl_u64)s_seg;
+    first = tile_start[sg];
+    local = tile - first;
+    const scl_u64 off = seg_off[sg];
+    n = seg_off[sg + 1] - off;
+    in += off;
+    out += off;
+    aligned = aligned && ((off * sizeof(scl_T)) % 16 == 0);
+    if (n == 0) return;  // an empty segment's only tile: nobody looks back at it
+  }
+  const scl_u64 base = local * TILE;
 
   // ---- stage the tile.  Full aligned tiles arrive by bulk copy in physical
   //      order: for a reverse scan the slot of logical vector q is then
@@ -427,15 +463,15 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
     }
     const scl_C aggc = (scl_C)carry;
     scl_C prefix = (scl_C)ident;
-    if (lane == 0) scl_publish(st, tile, tile == 0, aggc);
-    if (tile != 0) {
+    if (lane == 0) scl_publish(st, tile, tile == first, aggc);
+    if (tile != first) {
       scl_C running = (scl_C)ident;
       long long pred = (long long)tile - 1;
       while (true) {
         const long long idx = pred - lane;
         scl_C v = (scl_C)ident;
-        int kind = 2;
-        if (idx >= 0) {
+        int kind = 2;  // before the sequence's first tile: nothing to add
+        if (idx >= (long long)first) {
           kind = scl_poll(st, idx, spin_limit, &v);
           if (kind == 0) {
             scl_raise(err, SCL_DEV_ERR_TIMEOUT);

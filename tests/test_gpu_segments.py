@@ -1,0 +1,179 @@
+"""Segmented launches: thousands of uneven-length vectors stored back to back,
+one Scan / Reduce launch for all of them, against per-segment references
+(bit-exact for integers, FP64 oracle tolerances for floats)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import skelcl_gb300 as S
+
+pytestmark = pytest.mark.gpu
+
+IADD = "int func(int x, int y){ return x + y; }"
+FADD = "float func(float x, float y){ return x + y; }"
+
+
+def dev(a):
+    return S.DeviceArray.from_numpy(np.ascontiguousarray(a))
+
+
+def log_uniform_offsets(n_seg, lo, hi, seed, zeros=0):
+    rng = np.random.default_rng(seed)
+    lens = np.floor(2.0 ** rng.uniform(lo, hi, n_seg)).astype(np.uint64)
+    if zeros:
+        lens[rng.choice(n_seg, zeros, replace=False)] = 0
+    return np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+
+
+def seg_ids(off, n):
+    return np.searchsorted(off[1:], np.arange(n), side="right")
+
+
+def seg_scan_ref(x, off, flags):
+    """Per-segment scans of int32 x with wrap-around, all four flag forms."""
+    n = len(x)
+    x64 = x.astype(np.int64)
+    ids = seg_ids(off, n)
+    cs = np.cumsum(x64)
+    before = np.concatenate([[0], cs])[off[:-1].astype(np.int64)]  # sum before each segment
+    incl = cs - before[ids]
+    total = (np.concatenate([[0], cs])[off[1:].astype(np.int64)] - before)[ids]
+    if flags & 2:  # reverse: sum over [i, end of segment]
+        incl = total - incl + x64
+    res = incl if flags & 1 else incl - x64
+    return res.astype(np.int32)  # two's-complement wrap, as the int kernel
+
+
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+def test_segmented_scan_int_exact(scl, orc, flags):
+    off = log_uniform_offsets(3000, 0, 16, seed=1, zeros=50)  # 1 .. 65536 elements, some empty
+    n = int(off[-1])
+    x = orc.mod_i32(n, 2, 1001) - 500
+    p = S.Program(S.KIND_SCAN, IADD, ["int"], identity="0")
+    dy = S.DeviceArray(n, np.int32)
+    p.launch([dev(x), dy], n=n, flags=flags, segments=dev(off))
+    assert np.array_equal(dy.to_numpy(), seg_scan_ref(x, off, flags))
+
+
+def test_segmented_scan_single_segment_equals_plain(scl, orc):
+    n = 5_000_003
+    x = orc.mod_i32(n, 3, 1001)
+    p = S.Program(S.KIND_SCAN, IADD, ["int"], identity="0")
+    d1, d2 = S.DeviceArray(n, np.int32), S.DeviceArray(n, np.int32)
+    dx = dev(x)
+    p.launch([dx, d1], n=n, flags=S.SHAPE_INCLUSIVE, segments=dev(np.array([0, n], np.uint64)))
+    p.launch([dx, d2], n=n, flags=S.SHAPE_INCLUSIVE)
+    assert np.array_equal(d1.to_numpy(), d2.to_numpy())
+
+
+def test_segmented_scan_float(scl, orc):
+    off = log_uniform_offsets(2000, 6, 17, seed=4)
+    n = int(off[-1])
+    x = orc.uniform_f32(n, 5, -1.0, 1.0)
+    p = S.Program(S.KIND_SCAN, FADD, ["float"], identity="0")
+    dy = S.DeviceArray(n, np.float32)
+    p.launch([dev(x), dy], n=n, flags=S.SHAPE_INCLUSIVE, segments=dev(off))
+    ids = seg_ids(off, n)
+    cs = np.cumsum(x.astype(np.float64))
+    ref = cs - np.concatenate([[0.0], cs])[off[:-1].astype(np.int64)][ids]
+    pos = np.arange(n) - off[:-1].astype(np.int64)[ids] + 1  # terms summed
+    assert np.all(np.abs(dy.to_numpy() - ref) <= 1e-5 * (1.0 + np.sqrt(pos)))
+
+
+@pytest.mark.parametrize("dtype,src,types", [(np.int32, IADD, ["int"]), (np.float32, FADD, ["float"])])
+def test_segmented_reduce(scl, orc, dtype, src, types):
+    off = log_uniform_offsets(5000, 0, 17, seed=6, zeros=100)
+    n = int(off[-1])
+    x = (orc.mod_i32(n, 7, 1001) - 500).astype(dtype) if dtype == np.int32 else orc.uniform_f32(n, 7, -1.0, 1.0)
+    p = S.Program(S.KIND_REDUCE, src, types, identity="0")
+    dout = S.DeviceArray(len(off) - 1, dtype)
+    p.launch([dev(x), dout], n=n, segments=dev(off))
+    cs = np.concatenate([[0], np.cumsum(x.astype(np.int64 if dtype == np.int32 else np.float64))])
+    ref = cs[off[1:].astype(np.int64)] - cs[off[:-1].astype(np.int64)]
+    got = dout.to_numpy()
+    if dtype == np.int32:
+        assert np.array_equal(got, ref.astype(np.int32))
+    else:
+        lens = (off[1:] - off[:-1]).astype(np.float64)
+        assert np.all(np.abs(got - ref) <= 1e-6 * (1.0 + np.sqrt(lens)))
+    # a second launch on the same workspace (tickets were reset)
+    p.launch([dev(x), dout], n=n, segments=dev(off))
+    assert np.array_equal(dout.to_numpy(), got)
+
+
+def test_segmented_reduce_unaligned_and_empty(scl, orc):
+    off = np.array([0, 0, 1, 5, 5, 8200, 8201, 30001, 30001], np.uint64)
+    n = 30001
+    x = orc.mod_i32(n + 1, 8, 1001)
+    p = S.Program(S.KIND_REDUCE, IADD, ["int"], identity="0")
+    dout = S.DeviceArray(len(off) - 1, np.int32)
+    dx = dev(x).view(1, n)  # unaligned base
+    p.launch([dx, dout], n=n, segments=dev(off))
+    xs = x[1:].astype(np.int64)
+    ref = [int(xs[int(a):int(b)].sum()) for a, b in zip(off[:-1], off[1:])]
+    assert list(dout.to_numpy()) == ref
+
+
+def test_bad_offsets_are_clamped_and_reported(scl, orc):
+    n = 1000
+    x = orc.mod_i32(n, 9, 1001)
+    p = S.Program(S.KIND_REDUCE, IADD, ["int"], identity="0")
+    dout = S.DeviceArray(3, np.int32)
+    bad = np.array([0, 600, 300, 5000], np.uint64)  # decreasing, and past the end
+    p.launch([dev(x), dout], n=n, segments=dev(bad))
+    assert S.lib().scl_sync() == S.ERR_ARG
+    S.sync()  # status cleared, context usable
+    good = np.array([0, 600, 600, 1000], np.uint64)
+    p.launch([dev(x), dout], n=n, segments=dev(good))
+    xs = x.astype(np.int64)
+    assert list(dout.to_numpy()) == [int(xs[:600].sum()), 0, int(xs[600:].sum())]
+
+
+@pytest.mark.parametrize("dtype,code", [(np.float32, S.DTYPE_F32), (np.float64, S.DTYPE_F64)])
+def test_segmented_broadcast(scl, dtype, code):
+    off = log_uniform_offsets(777, 0, 14, seed=10, zeros=20)
+    n = int(off[-1])
+    g = np.arange(1, len(off), dtype=dtype)
+    gx = dev(np.full(n, 0.5, dtype))
+    dg, doff = dev(g), dev(off)  # keep the allocations alive across the launch
+    S.check(S.lib().scl_adjoint_broadcast_segments(dg.ptr, gx.ptr, doff.ptr, len(off) - 1, n, code, 1))
+    ids = seg_ids(off, n)
+    assert np.array_equal(gx.to_numpy(), (g[ids] + dtype(0.5)).astype(dtype))
+
+
+def test_segmented_pipeline_in_a_graph(scl, orc):
+    """Map(x*x+1) -> segmented inclusive Scan -> segmented Reduce, replayed from
+    a captured CUDA graph after one eager run (which sizes the workspaces)."""
+    off = log_uniform_offsets(1000, 6, 15, seed=11)
+    n = int(off[-1])
+    x = orc.uniform_f32(n, 12, -1.0, 1.0)
+    mp = S.Program(S.KIND_MAP, "float func(float x){ return x*x + 1.0f; }", ["float", "float"])
+    sp = S.Program(S.KIND_SCAN, FADD, ["float"], identity="0")
+    rp = S.Program(S.KIND_REDUCE, FADD, ["float"], identity="0")
+    dx, dm, ds = dev(x), S.DeviceArray(n, np.float32), S.DeviceArray(n, np.float32)
+    dr, doff = S.DeviceArray(len(off) - 1, np.float32), dev(off)
+
+    def step():
+        mp.launch([dx, dm], n=n)
+        sp.launch([dm, ds], n=n, flags=S.SHAPE_INCLUSIVE, segments=doff)
+        rp.launch([ds, dr], n=n, segments=doff)
+
+    step()
+    eager = dr.to_numpy().copy()
+    dr.upload(np.zeros(len(off) - 1, np.float32))
+    S.check(S.lib().scl_graph_begin())
+    step()
+    g = ctypes.c_void_p()
+    S.check(S.lib().scl_graph_end(ctypes.byref(g)))
+    S.check(S.lib().scl_graph_launch(g))
+    S.sync()
+    replay = dr.to_numpy()
+    S.check(S.lib().scl_graph_destroy(g))
+    m = x.astype(np.float64) ** 2 + 1.0
+    ids = seg_ids(off, n)
+    cs = np.cumsum(m)
+    scan = cs - np.concatenate([[0.0], cs])[off[:-1].astype(np.int64)][ids]
+    ref = np.bincount(ids, weights=scan, minlength=len(off) - 1)
+    assert np.all(np.abs(replay - ref) <= 1e-5 * np.abs(ref) + 1e-3)
+    assert np.allclose(replay, eager, rtol=1e-6)
