@@ -442,11 +442,111 @@ def secondary(S, oracle, hbm_peak, args):
                     source2="float func(float x, float y){ return fabs(x-y); }", identity="0")
     dL, dR, dM = S.DeviceArray.from_numpy(L_), S.DeviceArray.from_numpy(R_), S.DeviceArray(Ml * Nl, np.float32)
     ms = timed(S, lambda: man.launch([dL, dR, dM], rows=Ml, cols=Nl, dim=Kl), 5, 2)
+    out["segmented_10000_vectors"] = segmented(S, oracle, hbm_peak)
     out["manhattan_4096x256x4096"] = {"ms": round(ms, 3),
                                        "Gpairops": round(Ml * Nl * Kl / ms / 1e6, 1),
                                        "TFLOPs_3flop": round(3 * Ml * Nl * Kl / ms / 1e9, 2),
                                        "fp32_frac_nominal": round(3 * Ml * Nl * Kl / ms / 1e9 / fp32_peak, 3)}
     return out
+
+
+def segmented(S, oracle, hbm_peak):
+    """10,000 float32 vectors, lengths floor(2^U[6,20]) (seed 12), values
+    U[-1,1] (seed 13), back to back: Map(x*x+1) -> inclusive Scan(+) ->
+    Reduce(+) per vector, and the adjoints (segmented broadcast, segmented
+    reverse scan, Map's vector-Jacobian product).  One launch per skeleton
+    (plus the offsets pre-pass) for all vectors, replayed from a CUDA graph;
+    against the same pipeline on one flat vector of the same length and
+    against one launch per vector per skeleton (also replayed from a graph,
+    so host overhead is not counted)."""
+    import ctypes
+    L = S.lib()
+    nseg = 10_000
+    lens = np.floor(2.0 ** oracle.uniform_f32(nseg, 12, 6.0, 20.0).astype(np.float64)).astype(np.uint64)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+    n = int(off[-1])
+    x = oracle.uniform_f32(n, 13, -1.0, 1.0)
+    FADD = "float func(float x, float y){ return x + y; }"
+    mp = S.Program(S.KIND_MAP, "float func(float x){ return x*x + 1.0f; }", ["float", "float"])
+    ma = S.Program(S.KIND_MAP_ADJOINT, "float d(float x, float g){ return 2.0f*x*g; }", ["float", "float"], func="d")
+    sp = S.Program(S.KIND_SCAN, FADD, ["float"], identity="0")
+    rp = S.Program(S.KIND_REDUCE, FADD, ["float"], identity="0")
+    dx = S.DeviceArray.from_numpy(x)
+    dm, ds = S.DeviceArray(n, np.float32), S.DeviceArray(n, np.float32)
+    dgs, dgm, dgx = S.DeviceArray(n, np.float32), S.DeviceArray(n, np.float32), S.DeviceArray(n, np.float32)
+    doff = S.DeviceArray.from_numpy(off)
+    dr = S.DeviceArray(nseg, np.float32)
+    dseed = S.DeviceArray.from_numpy(np.ones(nseg, np.float32))
+    flat = S.DeviceArray.from_numpy(np.array([0, n], np.uint64))
+
+    def fwd(segs, out):
+        mp.launch([dx, dm], n=n)
+        sp.launch([dm, ds], n=n, flags=S.SHAPE_INCLUSIVE, segments=segs)
+        rp.launch([ds, out], n=n, segments=segs)
+
+    def adj(segs, nsegs):
+        S.check(L.scl_adjoint_broadcast_segments(dseed.ptr, dgs.ptr, segs.ptr, nsegs, n, S.DTYPE_F32, 0))
+        sp.launch([dgs, dgm], n=n, flags=S.SHAPE_INCLUSIVE | S.SHAPE_REVERSE, segments=segs)
+        ma.launch([dx, dgm, dgx], n=n)
+
+    def graph_of(fn):
+        fn()  # sizes the workspaces outside the capture
+        S.sync()
+        S.check(L.scl_graph_begin())
+        fn()
+        g = ctypes.c_void_p()
+        S.check(L.scl_graph_end(ctypes.byref(g)))
+        return g
+
+    def time_graph(g, reps):
+        return timed(S, lambda: S.check(L.scl_graph_launch(g)), reps, 2)
+
+    res = {"n_vectors": nseg, "elements": n, "mean_length": round(n / nseg, 1),
+           "bytes_per_elem_fwd_adjoint": [20, 24]}
+    g_fwd = graph_of(lambda: fwd(doff, dr))
+    g_adj = graph_of(lambda: adj(doff, nseg))
+    dr1 = S.DeviceArray(1, np.float32)
+    g_flat_fwd = graph_of(lambda: fwd(flat, dr1))
+    g_flat_adj = graph_of(lambda: adj(flat, 1))
+    f_ms, a_ms = time_graph(g_fwd, 10), time_graph(g_adj, 10)
+    ff_ms, fa_ms = time_graph(g_flat_fwd, 10), time_graph(g_flat_adj, 10)
+    res["segmented"] = {"fwd_ms": round(f_ms, 3), "adjoint_ms": round(a_ms, 3),
+                        "fwd_GBps": round(20 * n / f_ms / 1e6, 1), "adjoint_GBps": round(24 * n / a_ms / 1e6, 1),
+                        "fwd_frac": round(20 * n / f_ms / 1e6 / hbm_peak, 3),
+                        "fwd_plus_adjoint_over_fwd": round((f_ms + a_ms) / f_ms, 3)}
+    res["single_flat_vector"] = {"fwd_ms": round(ff_ms, 3), "adjoint_ms": round(fa_ms, 3),
+                                 "fwd_GBps": round(20 * n / ff_ms / 1e6, 1),
+                                 "adjoint_GBps": round(24 * n / fa_ms / 1e6, 1)}
+    res["segmented_over_single_bandwidth"] = {"fwd": round(ff_ms / f_ms, 3), "adjoint": round(fa_ms / a_ms, 3)}
+    # correctness on a sample of vectors (FP64)
+    fwd(doff, dr)
+    got = dr.to_numpy()
+    chk = np.arange(0, nseg, 97)
+    err = 0.0
+    for s_ in chk:
+        a, b = int(off[s_]), int(off[s_ + 1])
+        v = np.cumsum(x[a:b].astype(np.float64) ** 2 + 1.0).sum()
+        err = max(err, abs(float(got[s_]) - v) / abs(v))
+    res["max_rel_err_vs_fp64_sampled"] = err
+    for g in (g_fwd, g_adj, g_flat_fwd, g_flat_adj):
+        L.scl_graph_destroy(g)
+    # one launch per vector per skeleton, from a graph (forward only)
+    views = [(dx.view(int(off[i]), int(lens[i])), dm.view(int(off[i]), int(lens[i])),
+              ds.view(int(off[i]), int(lens[i])), dr.view(i, 1), int(lens[i])) for i in range(nseg)]
+
+    def per_vector():
+        for vx, vm, vs, vr, ln in views:
+            mp.launch([vx, vm], n=ln)
+            sp.launch([vm, vs], n=ln, flags=S.SHAPE_INCLUSIVE)
+            rp.launch([vs, vr], n=ln)
+
+    g_pv = graph_of(per_vector)
+    pv_ms = time_graph(g_pv, 2)
+    L.scl_graph_destroy(g_pv)
+    res["per_vector_launches"] = {"launches": 3 * nseg, "fwd_ms": round(pv_ms, 3),
+                                  "fwd_GBps": round(20 * n / pv_ms / 1e6, 1),
+                                  "segmented_speedup": round(pv_ms / f_ms, 2)}
+    return res
 
 
 def run_reference(args):

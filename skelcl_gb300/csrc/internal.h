@@ -157,9 +157,11 @@ int launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, ArgPack& pack);
 // generated kernels).
 constexpr unsigned int kDevErrSegments = 2u;  // segment offsets decreasing or past the end
 // Pre-pass of segmented launches (segments.cu): sanitised offsets and the
-// first tile of every segment (tile_start[n_seg] = tile count).
+// first tile of every segment (tile_start[n_seg] = tile count); tiles of
+// `tile` elements laid on the grid {a + k*vg} (vg = 1: from the segment start).
 int segments_prepare(const uint64_t* seg_offsets, uint64_t n_seg, uint64_t n_total, uint64_t tile,
-                     uint64_t* off_out, unsigned int* tile_start, cudaStream_t stream);
+                     uint64_t vg, uint64_t a, int reverse, uint64_t* off_out,
+                     unsigned int* tile_start, cudaStream_t stream);
 // Autotuner lookup/store; returns false when nothing is cached.
 bool tune_lookup(const std::string& key, scl_tuning* out);
 void tune_store(const std::string& key, const scl_tuning& t);

@@ -313,11 +313,12 @@ extern "C" int scl_launch_reduce(scl_program* p, const scl_shape* sh, void* cons
     // one result per segment, one launch (plus the offsets pre-pass)
     if (!sh->seg_offsets) return fail(SCL_ERR_ARG, "segmented reduce: null seg_offsets");
     uint64_t n_seg = sh->n_segments;
-    const uint64_t tile = 8ull * 256 * V;
+    // 128 KB tiles for 16-byte vectors: few blocks, each with long streams of loads
+    const uint64_t tile = 32ull * 256 * V;
     const uint64_t tiles = (n + tile - 1) / tile + n_seg;
     if (tiles > 0x7fffffffull) return fail(SCL_ERR_ARG, "segmented reduce: too many tiles");
-    CUfunction fn = find_kernel(p, "scl_reduce_seg<8>");
-    if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_reduce_seg<8> missing");
+    CUfunction fn = find_kernel(p, "scl_reduce_seg<32>");
+    if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_reduce_seg<32> missing");
     auto up = [](size_t b) { return (b + 255) / 256 * 256; };
     const size_t tk = up(n_seg * 4), pa = up(tiles * csz), of = up((n_seg + 1) * 8);
     if (int st = ensure_workspace(p, tk + pa + of + up((n_seg + 1) * 4))) return st;
@@ -327,7 +328,7 @@ extern "C" int scl_launch_reduce(scl_program* p, const scl_shape* sh, void* cons
     void* offs = ws + tk + pa;
     void* tstart = ws + tk + pa + of;
     SCL_CUDA(cudaMemsetAsync(tickets, 0, tk, rt().stream));
-    if (int st = segments_prepare(sh->seg_offsets, n_seg, n, tile, (uint64_t*)offs,
+    if (int st = segments_prepare(sh->seg_offsets, n_seg, n, tile, 1, 0, 0, (uint64_t*)offs,
                                   (unsigned int*)tstart, rt().stream))
       return st;
     unsigned int* err = rt().dev_err;
@@ -377,7 +378,6 @@ extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const*
   unsigned int flags = sh->flags & (SCL_SHAPE_INCLUSIVE | SCL_SHAPE_REVERSE);
   const bool reverse = (flags & SCL_SHAPE_REVERSE) != 0;
   int aligned = (aligned16(in) && aligned16(out)) ? 1 : 0;
-  (void)reverse;
   // 32 KB tiles by default: fewer tiles to look back over (measured on GB300)
   uint32_t R = (tu && tu->items) ? tu->items : 8;
   if (R != 2 && R != 4 && R != 8 && R != 16) R = 8;
@@ -401,7 +401,21 @@ extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const*
       return fail(SCL_ERR_UNSUPPORTED, "segmented scan: the tile does not fit in shared memory");
   }
   const uint64_t tile = (uint64_t)R * 256 * V;
-  const uint64_t tiles = (n + tile - 1) / tile + n_seg;  // segmented: an upper bound
+  // the staged kernel lays tiles on the 16-byte grid of `in` (first element
+  // index a on a boundary, every vg elements); the same rule counts them here
+  const bool grid = staged && (tsz == 4 || tsz == 8 || tsz == 16) &&
+                    reinterpret_cast<uintptr_t>(in) % tsz == 0;
+  const uint64_t vg = grid ? (uint64_t)V : 1;
+  const uint64_t ga = grid ? ((16u - (reinterpret_cast<uintptr_t>(in) & 15u)) & 15u) / tsz : 0;
+  uint64_t tiles;
+  if (n_seg) {
+    tiles = (n + tile - 1) / tile + 2 * n_seg;  // an upper bound; the pre-pass has the count
+  } else if (staged) {
+    const uint64_t m = reverse ? (ga + vg - n % vg) % vg : (vg - ga) % vg;
+    tiles = (n + m + tile - 1) / tile;
+  } else {
+    tiles = (n + tile - 1) / tile;
+  }
   if (tiles > 0x7fffffffull) return fail(SCL_ERR_ARG, "scan input too large");
   // resident tiles per SM the register (or shared-memory) budget is sized for
   uint32_t minb = (tu && tu->tile_w) ? tu->tile_w : 0;
@@ -448,8 +462,8 @@ extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const*
   void* tile_start = n_seg ? (char*)p->ws.ptr + total + seg_of : nullptr;
   SCL_CUDA(cudaMemsetAsync(p->ws.ptr, 0, clear_bytes, rt().stream));
   if (n_seg) {
-    if (int st = segments_prepare(sh->seg_offsets, n_seg, n, tile, (uint64_t*)seg_off,
-                                  (unsigned int*)tile_start, rt().stream))
+    if (int st = segments_prepare(sh->seg_offsets, n_seg, n, tile, vg, ga, reverse ? 1 : 0,
+                                  (uint64_t*)seg_off, (unsigned int*)tile_start, rt().stream))
       return st;
   }
   unsigned int spin = spin_of(tu);

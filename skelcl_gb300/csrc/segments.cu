@@ -6,9 +6,13 @@
 // copies the caller's offsets into the program workspace clamped to the
 // buffer and made non-decreasing (raising a device status bit if they were
 // not), and numbers the tiles: segment s owns tiles tile_start[s] ..
-// tile_start[s+1]-1, max(1, ceil(len / tile)) of them, so no tile spans two
-// segments.  tile_start[n_segments] is the tile count.
+// tile_start[s+1]-1, so no tile spans two segments: max(1, ceil(len / tile))
+// of them, or, for tiles laid on a grid of vg elements with phase a (the
+// scan's 16-byte grid), as many as cover the segment once its start (end,
+// for a reverse scan) is rounded onto the grid.  tile_start[n_segments] is
+// the tile count.
 #include <cstdint>
+#include <cstring>
 
 #include "internal.h"
 
@@ -58,7 +62,8 @@ __device__ uint64_t block_incl(uint64_t v, uint64_t* s_warp) {
 
 __global__ void __launch_bounds__(kPrepThreads)
 segments_prepare_kernel(const uint64_t* off_in, uint64_t n_seg, uint64_t n_total, uint64_t tile,
-                        uint64_t* off_out, unsigned int* tile_start, unsigned int* err) {
+                        uint64_t vg, uint64_t a, int reverse, uint64_t* off_out,
+                        unsigned int* tile_start, unsigned int* err) {
   __shared__ uint64_t s_warp[32];
   __shared__ uint64_t s_carry;
   __shared__ int s_bad;
@@ -96,8 +101,10 @@ segments_prepare_kernel(const uint64_t* off_in, uint64_t n_seg, uint64_t n_total
     const uint64_t s = c + threadIdx.x;
     uint64_t cnt = 0;
     if (s < n_seg) {
-      const uint64_t len = off_out[s + 1] - off_out[s];
-      cnt = len == 0 ? 1 : (len + tile - 1) / tile;
+      const uint64_t lo = off_out[s], hi = off_out[s + 1];
+      // the segment's first tile starts (ends, reverse) on the grid {a + k*vg}
+      const uint64_t m = reverse ? (a + vg - hi % vg) % vg : (lo + vg - a) % vg;
+      cnt = hi == lo ? 1 : (hi - lo + m + tile - 1) / tile;
     }
     const uint64_t incl = block_incl<false>(cnt, s_warp);
     const uint64_t carry = s_carry;
@@ -113,14 +120,17 @@ segments_prepare_kernel(const uint64_t* off_in, uint64_t n_seg, uint64_t n_total
 }
 
 // gx[i] (+)= g[s] for every element i of segment s (elements outside every
-// segment are left alone).  Each block takes a chunk of the buffer; its
-// threads walk the offsets forward from the chunk's first segment.
+// segment are left alone).  Each block takes a chunk of CH elements; its
+// threads walk the offsets forward from the chunk's first segment.  With a
+// 16-byte aligned gx, a vector of 16 bytes inside one segment is written with
+// one store.
 template <typename T>
 __global__ void broadcast_segments_kernel(const T* __restrict__ g, T* __restrict__ gx,
                                           const uint64_t* __restrict__ off, uint64_t n_seg,
-                                          uint64_t n_total, int acc) {
-  constexpr int CH = 4096;
+                                          uint64_t n_total, int acc, int aligned) {
+  constexpr int CH = 8192, V = 16 / sizeof(T);
   const uint64_t c0 = (uint64_t)blockIdx.x * CH;
+  const uint64_t c1 = c0 + CH < n_total ? c0 + CH : n_total;
   __shared__ uint64_t s_first;
   if (threadIdx.x == 0) {
     // last segment s with off[s] <= c0 (0 if none)
@@ -133,22 +143,48 @@ __global__ void broadcast_segments_kernel(const T* __restrict__ g, T* __restrict
   }
   __syncthreads();
   uint64_t s = s_first;
-  for (int k = threadIdx.x; k < CH; k += blockDim.x) {
-    const uint64_t i = c0 + k;
-    if (i >= n_total) break;
+  auto one = [&](uint64_t i) {
     while (s + 1 < n_seg && i >= off[s + 1]) ++s;
-    if (i < off[s] || i >= off[s + 1]) continue;
+    if (i < off[s] || i >= off[s + 1]) return;
     const T v = g[s];
     gx[i] = acc ? gx[i] + v : v;
+  };
+  if (!aligned) {
+    for (uint64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) one(i);
+    return;
+  }
+  for (uint64_t i = c0 + (uint64_t)threadIdx.x * V; i < c1; i += (uint64_t)blockDim.x * V) {
+    while (s + 1 < n_seg && i >= off[s + 1]) ++s;
+    if (i + V <= c1 && i >= off[s] && i + V <= off[s + 1]) {
+      const T v = g[s];
+      T r[V];
+      if (acc) {
+        const uint4 q = *reinterpret_cast<const uint4*>(gx + i);
+        memcpy(r, &q, 16);
+#pragma unroll
+        for (int e = 0; e < V; ++e) r[e] += v;
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) r[e] = v;
+      }
+      uint4 q;
+      memcpy(&q, r, 16);
+      *reinterpret_cast<uint4*>(gx + i) = q;
+    } else {
+      const uint64_t s_keep = s;
+      for (int e = 0; e < V && i + e < c1; ++e) one(i + e);
+      s = s_keep;
+    }
   }
 }
 
 }  // namespace
 
 int segments_prepare(const uint64_t* seg_offsets, uint64_t n_seg, uint64_t n_total, uint64_t tile,
-                     uint64_t* off_out, unsigned int* tile_start, cudaStream_t stream) {
-  segments_prepare_kernel<<<1, kPrepThreads, 0, stream>>>(seg_offsets, n_seg, n_total, tile, off_out,
-                                                          tile_start, rt().dev_err);
+                     uint64_t vg, uint64_t a, int reverse, uint64_t* off_out,
+                     unsigned int* tile_start, cudaStream_t stream) {
+  segments_prepare_kernel<<<1, kPrepThreads, 0, stream>>>(seg_offsets, n_seg, n_total, tile, vg, a,
+                                                          reverse, off_out, tile_start, rt().dev_err);
   SCL_CUDA(cudaGetLastError());
   ++rt().launches;
   return SCL_OK;
@@ -166,15 +202,16 @@ extern "C" int scl_adjoint_broadcast_segments(const void* g, void* gx, const uin
     return fail(SCL_ERR_ARG, "segmented broadcast: dtype must be SCL_DTYPE_F32 or _F64");
   if (n == 0 || n_segments == 0) return SCL_OK;
   if (!g || !gx || !seg_offsets) return fail(SCL_ERR_ARG, "segmented broadcast: null pointer");
-  const uint64_t blocks = (n + 4095) / 4096;
+  const uint64_t blocks = (n + 8191) / 8192;
   if (blocks > 0x7fffffffull) return fail(SCL_ERR_ARG, "segmented broadcast: vector too large");
   const int acc = accumulate ? 1 : 0;
+  const int aligned = (reinterpret_cast<uintptr_t>(gx) & 15u) == 0 ? 1 : 0;
   if (dtype == SCL_DTYPE_F32)
     broadcast_segments_kernel<float><<<(unsigned)blocks, 256, 0, rt().stream>>>(
-        (const float*)g, (float*)gx, seg_offsets, n_segments, n, acc);
+        (const float*)g, (float*)gx, seg_offsets, n_segments, n, acc, aligned);
   else
     broadcast_segments_kernel<double><<<(unsigned)blocks, 256, 0, rt().stream>>>(
-        (const double*)g, (double*)gx, seg_offsets, n_segments, n, acc);
+        (const double*)g, (double*)gx, seg_offsets, n_segments, n, acc, aligned);
   SCL_CUDA(cudaGetLastError());
   ++rt().launches;
   return SCL_OK;

@@ -240,20 +240,45 @@ scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
   bool have = false;
   scl_T acc;
   const bool vec = aligned && ((off * sizeof(scl_T)) % 16 == 0) && end - begin == TILE;
-  if (vec) {
-    scl_pack<scl_T, V> a[R];
+  if (vec) {  // R vectors per thread, loaded 8 at a time
+    constexpr int G = R < 8 ? R : 8;
+#pragma unroll 1
+    for (int r0 = 0; r0 < R; r0 += G) {
+      scl_pack<scl_T, V> a[G];
 #pragma unroll
-    for (int r = 0; r < R; ++r) a[r] = scl_load<scl_T, V>(src + begin + ((scl_u64)r * B + threadIdx.x) * V);
-    acc = a[0].v[0];
+      for (int r = 0; r < G; ++r)
+        a[r] = scl_load<scl_T, V>(src + begin + ((scl_u64)(r0 + r) * B + threadIdx.x) * V);
 #pragma unroll
-    for (int e = 1; e < V; ++e) acc = SCL_FUNC(acc, a[0].v[e] SCL_EXTRA_ARGS);
+      for (int r = 0; r < G; ++r)
 #pragma unroll
-    for (int r = 1; r < R; ++r)
-#pragma unroll
-      for (int e = 0; e < V; ++e) acc = SCL_FUNC(acc, a[r].v[e] SCL_EXTRA_ARGS);
-    have = true;
+        for (int e = 0; e < V; ++e) {
+          acc = have ? SCL_FUNC(acc, a[r].v[e] SCL_EXTRA_ARGS) : a[r].v[e];
+          have = true;
+        }
+    }
   } else {
-    for (scl_u64 i = begin + threadIdx.x; i < end; i += B) {
+    // ragged or unaligned: scalar head up to the first 16-byte boundary,
+    // 16-byte body, scalar tail
+    scl_u64 h = begin, bend = begin;
+    if (V > 1 && ((scl_u64)(src + begin)) % sizeof(scl_T) == 0) {
+      const scl_u64 mis = ((scl_u64)(src + begin)) & 15u;
+      h = begin + (mis ? (16u - mis) / sizeof(scl_T) : 0);
+      if (h > end) h = end;
+      bend = h + (end - h) / V * V;
+    }
+    for (scl_u64 i = begin + threadIdx.x; i < h; i += B) {
+      acc = have ? SCL_FUNC(acc, src[i] SCL_EXTRA_ARGS) : src[i];
+      have = true;
+    }
+    for (scl_u64 i = h + (scl_u64)threadIdx.x * V; i < bend; i += (scl_u64)B * V) {
+      scl_pack<scl_T, V> a = scl_load<scl_T, V>(src + i);
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        acc = have ? SCL_FUNC(acc, a.v[e] SCL_EXTRA_ARGS) : a.v[e];
+        have = true;
+      }
+    }
+    for (scl_u64 i = (bend > h ? bend : h) + threadIdx.x; i < end; i += B) {
       acc = have ? SCL_FUNC(acc, src[i] SCL_EXTRA_ARGS) : src[i];
       have = true;
     }

@@ -320,12 +320,22 @@ __device__ __forceinline__ bool scl_mbar_wait(unsigned int bar_s, unsigned int s
 }
 
 //
+// Tiles lie on the 16-byte grid of `in`: with `a` the first element index on
+// a 16-byte boundary, a (forward) sequence [lo, hi) starts its first tile at
+// lo rounded down onto the grid, and a reverse sequence ends its first tile
+// at hi rounded up; elements of a tile outside the sequence are masked with
+// the identity (which must be neutral, as for the reference's padding).  So
+// every tile's shared-memory image has position p <-> element tile_lo + p,
+// 16-byte vector slots, and one bulk copy of the tile's elements, rounded
+// out to 16 bytes, when that stays inside the vector.  Elements that cannot
+// be aligned (sizes other than 4, 8, 16 bytes, or a misaligned pointer) use
+// ordinary loads.  The host counts tiles with the same rule (scl_scan_tiles).
+//
 // SEG = 1: a segmented scan, one independent scan per segment
-// [seg_off[s], seg_off[s+1]) of the flat vector.  Tiles never span segments:
-// segment s owns the tickets tile_start[s] .. tile_start[s+1]-1 (at least
-// one), a tile works on its segment with segment-relative pointers, and the
-// look-back stops at the segment's first tile.  Tickets past the last tile
-// (the grid is an upper bound) return at once.
+// [seg_off[s], seg_off[s+1]) of the flat vector.  Segment s owns the tickets
+// tile_start[s] .. tile_start[s+1]-1 (at least one), and the look-back stops
+// at the segment's first tile.  Tickets past the last tile (the grid is an
+// upper bound) return at once.
 template <int R, int MINB, int SEG = 0>
 __global__ void __launch_bounds__(SCL_SCAN_B, MINB)
 scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int aligned,
@@ -333,14 +343,16 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
            unsigned int* err, const scl_u64* seg_off, const unsigned int* tile_start,
            scl_u64 n_seg SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
+  (void)aligned;
   constexpr int B = SCL_SCAN_B, W = SCL_SCAN_W;
   constexpr int V = scl_vec_width<sizeof(scl_T)>::value;
   constexpr int TILE = R * B * V;
   constexpr unsigned int ROW_BYTES = B * V * sizeof(scl_T);
+  constexpr bool natural = sizeof(scl_T) == 4 || sizeof(scl_T) == 8 || sizeof(scl_T) == 16;
   const bool inclusive = (flags & 1u) != 0, reverse = (flags & 2u) != 0;
   const scl_T ident = (scl_T)(SCL_IDENTITY);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  scl_T* ts = reinterpret_cast<scl_T*>(scl_dyn_smem);  // the tile, logical order
+  scl_T* ts = reinterpret_cast<scl_T*>(scl_dyn_smem);  // position p <-> element tile_lo + p
 
   __shared__ __align__(8) unsigned long long bar;
   __shared__ unsigned int s_tile;
@@ -356,18 +368,18 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
   __syncthreads();
   const unsigned int tile = s_tile;
   unsigned int first = 0;  // ticket of the first tile of this tile's sequence
-  scl_u64 local = tile;    // tile index within the sequence
+  long long lo = 0, hi = (long long)n;  // the sequence's elements
   if constexpr (SEG != 0) {
     __shared__ long long s_seg;
     if (threadIdx.x == 0) {
       long long sg = -1;
       if (tile < tile_start[n_seg]) {
-        scl_u64 lo = 0, hi = n_seg - 1;  // largest s with tile_start[s] <= tile
-        while (lo < hi) {
-          const scl_u64 mid = (lo + hi + 1) / 2;
-          if (tile_start[mid] <= tile) lo = mid; else hi = mid - 1;
+        scl_u64 l = 0, h = n_seg - 1;  // largest s with tile_start[s] <= tile
+        while (l < h) {
+          const scl_u64 mid = (l + h + 1) / 2;
+          if (tile_start[mid] <= tile) l = mid; else h = mid - 1;
         }
-        sg = (long long)lo;
+        sg = (long long)l;
       }
       s_seg = sg;
     }
@@ -375,34 +387,59 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
     if (s_seg < 0) return;
     const scl_u64 sg = (scl_u64)s_seg;
     first = tile_start[sg];
-    local = tile - first;
-    const scl_u64 off = seg_off[sg];
-    n = seg_off[sg + 1] - off;
-    in += off;
-    out += off;
-    aligned = aligned && ((off * sizeof(scl_T)) % 16 == 0);
-    if (n == 0) return;  // an empty segment's only tile: nobody looks back at it
+    lo = (long long)seg_off[sg];
+    hi = (long long)seg_off[sg + 1];
+    if (lo == hi) return;  // an empty segment's only tile: nobody looks back at it
   }
-  const scl_u64 base = local * TILE;
+  const long long local = (long long)(tile - first);
 
-  // ---- stage the tile.  Full aligned tiles arrive by bulk copy in physical
-  //      order: for a reverse scan the slot of logical vector q is then
-  //      TILE - (q+1)*V with its elements reversed; the in-thread pass below
-  //      rewrites every slot in logical order.
-  const bool bulk = aligned && base + TILE <= n && (!reverse || n % V == 0);
-  const bool rev_slots = bulk && reverse;
+  // ---- the tile's place on the grid, its valid elements [c_lo, c_hi)
+  const bool grid = natural && ((scl_u64)in % sizeof(scl_T)) == 0;
+  const long long vg = grid ? V : 1;
+  const long long a = grid ? (long long)(((16u - ((scl_u64)in & 15u)) & 15u) / sizeof(scl_T)) : 0;
+  long long tile_lo;
+  if (!reverse) {
+    const long long m = (((lo - a) % vg) + vg) % vg;
+    tile_lo = lo - m + local * TILE;
+  } else {
+    const long long m = (((a - hi) % vg) + vg) % vg;
+    tile_lo = hi + m - (local + 1) * TILE;
+  }
+  const long long c_lo = tile_lo > lo ? tile_lo : lo;
+  const long long c_hi = tile_lo + TILE < hi ? tile_lo + TILE : hi;
+  const bool full = c_lo == tile_lo && c_hi == tile_lo + TILE;
+
+  // ---- stage: one bulk copy of [c_lo, c_hi) rounded out to 16 bytes, or loads
+  const scl_u64 tbase = (scl_u64)in + (scl_u64)(tile_lo * (long long)sizeof(scl_T));
+  const scl_u64 g0 = (scl_u64)in + (scl_u64)c_lo * sizeof(scl_T);
+  const scl_u64 g1 = (scl_u64)in + (scl_u64)c_hi * sizeof(scl_T);
+  const scl_u64 a0 = g0 & ~(scl_u64)15, a1 = (g1 + 15) & ~(scl_u64)15;
+  const scl_u64 vlo = ((scl_u64)in + 15) & ~(scl_u64)15;
+  const scl_u64 vhi = ((scl_u64)in + (scl_u64)n * sizeof(scl_T)) & ~(scl_u64)15;
+  const bool bulk = grid && a0 >= vlo && a1 <= vhi;
   if (bulk) {
-    const scl_T* src = reverse ? in + (n - base - TILE) : in + base;
     if (threadIdx.x == 0) {
+      const unsigned int bytes = (unsigned int)(a1 - a0);
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                   :: "r"(bar_s), "r"((unsigned int)(TILE * sizeof(scl_T))) : "memory");
-      const unsigned int dst = (unsigned int)__cvta_generic_to_shared(ts);
+                   :: "r"(bar_s), "r"(bytes) : "memory");
+      const unsigned int dst = (unsigned int)__cvta_generic_to_shared(ts) + (unsigned int)(a0 - tbase);
+      if (full) {
 #pragma unroll
-      for (int r = 0; r < R; ++r)
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-            :: "r"(dst + r * ROW_BYTES), "l"(src + (scl_u64)r * B * V), "r"(ROW_BYTES), "r"(bar_s)
-            : "memory");
+        for (int r = 0; r < R; ++r)
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+              :: "r"(dst + r * ROW_BYTES), "l"((const void*)(a0 + r * ROW_BYTES)), "r"(ROW_BYTES),
+                 "r"(bar_s)
+              : "memory");
+      } else {
+        for (unsigned int o = 0; o < bytes; o += ROW_BYTES) {
+          const unsigned int sz = bytes - o < ROW_BYTES ? bytes - o : ROW_BYTES;
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+              :: "r"(dst + o), "l"((const void*)(a0 + o)), "r"(sz), "r"(bar_s)
+              : "memory");
+        }
+      }
       const bool ok = scl_mbar_wait(bar_s, spin_limit);
       if (!ok) {
         scl_raise(err, SCL_DEV_ERR_TIMEOUT);
@@ -417,21 +454,30 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
     if (!s_ok) return;  // successors time out too and see the error flag
   } else {
     for (int k = threadIdx.x; k < TILE; k += B) {
-      const scl_u64 i = base + k;
-      ts[k] = i < n ? in[reverse ? n - 1 - i : i] : ident;
+      const long long i = tile_lo + k;
+      ts[k] = (i >= c_lo && i < c_hi) ? in[i] : ident;
     }
     __syncthreads();
   }
+  const bool mask = bulk && !full;  // positions outside [c_lo, c_hi) hold other data
 
-  // ---- in-thread inclusive scan of each vector (kept in shared memory),
-  //      warp scans of the vector totals
+  // ---- in-thread inclusive scan of each logical vector (written back to its
+  //      slot in logical order), warp scans of the vector totals.  Logical
+  //      vector q sits at q*V, or at TILE-(q+1)*V reversed for a reverse scan.
   scl_T wincl[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int q = r * B + threadIdx.x;
-    scl_T* vp = ts + (rev_slots ? TILE - (q + 1) * V : q * V);
-    scl_pack<scl_T, V> p = scl_load<scl_T, V>(vp);
-    if (rev_slots) {
+    const int pos = reverse ? TILE - (q + 1) * V : q * V;
+    scl_pack<scl_T, V> p = scl_load<scl_T, V>(ts + pos);
+    if (mask) {
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        const long long i = tile_lo + pos + e;
+        if (i < c_lo || i >= c_hi) p.v[e] = ident;
+      }
+    }
+    if (reverse) {
 #pragma unroll
       for (int e = 0; e < V / 2; ++e) {
         const scl_T t = p.v[e];
@@ -441,7 +487,7 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
     }
 #pragma unroll
     for (int e = 1; e < V; ++e) p.v[e] = SCL_FUNC(p.v[e - 1], p.v[e] SCL_EXTRA_ARGS);
-    scl_store<scl_T, V>(vp, p);
+    scl_store<scl_T, V>(ts + pos, p);
     wincl[r] = scl_warp_incl(p.v[V - 1] SCL_EXTRA_ARGS);
     if (lane == 31) s_wsum[r * W + warp] = wincl[r];
   }
@@ -480,8 +526,8 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
           }
         }
         const unsigned int pmask = __ballot_sync(0xffffffffu, kind == 2);
-        const int first = pmask ? __ffs(pmask) - 1 : 31;
-        if (lane > first) v = (scl_C)ident;
+        const int first_inc = pmask ? __ffs(pmask) - 1 : 31;
+        if (lane > first_inc) v = (scl_C)ident;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
           scl_C o = scl_shfl_down(v, off);
@@ -499,18 +545,19 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
   }
   __syncthreads();
 
-  // ---- outputs
+  // ---- outputs: 16-byte stores for whole slots when `out` shares the grid
   const scl_T tile_carry = (scl_T)s_prefix;
-  const bool vec_out = aligned && base + TILE <= n && (!reverse || n % V == 0);
+  const bool ovec = full && (((scl_u64)out + (scl_u64)(tile_lo * (long long)sizeof(scl_T))) & 15u) == 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const scl_u64 q = (scl_u64)r * B + threadIdx.x;
-    scl_pack<scl_T, V> p = scl_load<scl_T, V>(ts + (rev_slots ? TILE - (q + 1) * V : q * V));
+    const int q = r * B + threadIdx.x;
+    const int pos = reverse ? TILE - (q + 1) * V : q * V;
+    scl_pack<scl_T, V> p = scl_load<scl_T, V>(ts + pos);
     scl_T lane_excl = scl_shfl_up(wincl[r], 1);
     if (lane == 0) lane_excl = ident;
     const scl_T pre = SCL_FUNC(SCL_FUNC(tile_carry, s_wsum[r * W + warp] SCL_EXTRA_ARGS),
                                lane_excl SCL_EXTRA_ARGS);
-    scl_pack<scl_T, V> o;
+    scl_pack<scl_T, V> o;  // logical order
     if (inclusive) {
 #pragma unroll
       for (int e = 0; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e] SCL_EXTRA_ARGS);
@@ -519,20 +566,21 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
 #pragma unroll
       for (int e = 1; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e - 1] SCL_EXTRA_ARGS);
     }
-    if (vec_out) {
-      if (!reverse) {
-        scl_store<scl_T, V>(out + base + q * V, o);
-      } else {
-        scl_pack<scl_T, V> rv;
+    if (reverse) {  // back to physical order
 #pragma unroll
-        for (int e = 0; e < V; ++e) rv.v[V - 1 - e] = o.v[e];
-        scl_store<scl_T, V>(out + (n - base - (q + 1) * V), rv);
+      for (int e = 0; e < V / 2; ++e) {
+        const scl_T t = o.v[e];
+        o.v[e] = o.v[V - 1 - e];
+        o.v[V - 1 - e] = t;
       }
+    }
+    if (ovec) {
+      scl_store<scl_T, V>(out + (tile_lo + pos), o);
     } else {
 #pragma unroll
       for (int e = 0; e < V; ++e) {
-        const scl_u64 i = base + q * V + e;
-        if (i < n) out[reverse ? n - 1 - i : i] = o.v[e];
+        const long long i = tile_lo + pos + e;
+        if (i >= c_lo && i < c_hi) out[i] = o.v[e];
       }
     }
   }
