@@ -288,6 +288,17 @@ int scl_adjoint_accumulate(void* dst, const void* src, uint64_t n, int dtype);
 int scl_mapoverlap_adjoint_edges(const float* g, const float* w, float* gin, uint64_t rows,
                                  uint64_t cols, int R);
 
+/* ---- autotuner (no counterpart in the reference).  With mode 1 (or
+ *      SKELCL_AUTOTUNE=1), a launch given no tuning (NULL or only spin_limit)
+ *      whose outputs overlap none of its inputs is timed once per (device,
+ *      program, skeleton, log2 size) over a few block sizes / items per thread
+ *      (Map, Zip, Reduce), tile shapes (Scan, segmented Scan and Reduce) or
+ *      rows per thread and staging (MapOverlap); the fastest is cached in
+ *      memory and in SKELCL_CACHE_DIR/autotune.tsv.  Not during a graph
+ *      capture: run the sequence once before capturing it. */
+int scl_autotune_set(int mode);
+int scl_autotune_get(int* mode);
+
 /* Variant the last launch of `prog` used (SCL_VARIANT_*). */
 int scl_program_last_variant(const scl_program* prog, uint32_t* variant);
 /* Kernels this library launched since scl_init (all programs). */

@@ -106,6 +106,7 @@ SIGNATURES = {
     "scl_adjoint_broadcast": ([_VP, _VP, _U64, _I, _I], _I),
     "scl_adjoint_accumulate": ([_VP, _VP, _U64, _I], _I),
     "scl_adjoint_broadcast_segments": ([_VP, _VP, _VP, _U64, _U64, _I, _I], _I),
+    "scl_autotune_set": ([_I], _I), "scl_autotune_get": ([ctypes.POINTER(_I)], _I),
     "scl_mapoverlap_adjoint_edges": ([_VP, _VP, _VP, _U64, _U64, _I], _I),
 }
 

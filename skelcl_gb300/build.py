@@ -29,7 +29,7 @@ ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 TEMPLATES = ["prelude", "elementwise", "reduce", "scan", "mapoverlap_pre", "mapoverlap",
              "allpairs_pre", "allpairs"]
-SOURCES = ["runtime.cu", "program.cpp", "splicer.cpp", "launch.cpp", "allpairs_tc.cu", "noalloc.cu", "adjoint.cu", "segments.cu"]
+SOURCES = ["runtime.cu", "program.cpp", "splicer.cpp", "launch.cpp", "allpairs_tc.cu", "noalloc.cu", "adjoint.cu", "segments.cu", "tune.cpp"]
 
 
 def _cuda_home() -> Path:

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -162,10 +163,15 @@ constexpr unsigned int kDevErrSegments = 2u;  // segment offsets decreasing or p
 int segments_prepare(const uint64_t* seg_offsets, uint64_t n_seg, uint64_t n_total, uint64_t tile,
                      uint64_t vg, uint64_t a, int reverse, uint64_t* off_out,
                      unsigned int* tile_start, cudaStream_t stream);
-// Autotuner lookup/store; returns false when nothing is cached.
+// Autotuner (tune.cpp): lookup/store of the (device, program, skeleton, size
+// bucket) cache, and the launch wrapper that times `cands` on a miss.
 bool tune_lookup(const std::string& key, scl_tuning* out);
 void tune_store(const std::string& key, const scl_tuning& t);
 bool autotune_enabled();
+bool untuned(const scl_tuning* t);  // null or only spin_limit set
+int tuned_launch(scl_program* p, const char* skel, uint64_t size, const scl_tuning* tu, bool safe,
+                 const std::vector<scl_tuning>& cands,
+                 const std::function<int(const scl_tuning*)>& run);
 }  // namespace scl
 
 #endif  // SKELCL_GB300_INTERNAL_H_

@@ -178,7 +178,8 @@ int check_prog(scl_program* p, std::initializer_list<int> kinds) {
 using namespace scl;
 
 // ---- Map / Zip ----------------------------------------------------------------
-extern "C" int scl_launch_map(scl_program* p, const scl_shape* sh, void* const* bufs,
+// (the exported scl_launch_* are the autotuning wrappers at the end of this file)
+static int launch_map_impl(scl_program* p, const scl_shape* sh, void* const* bufs,
                               const void* extra, size_t extra_bytes, const scl_tuning* tu) {
   if (int st = check_prog(p, {SCL_KIND_MAP, SCL_KIND_MAP_VOID, SCL_KIND_MAP_INDEX,
                               SCL_KIND_MAP_INDEX_VOID, SCL_KIND_MAP_POINT,
@@ -299,7 +300,7 @@ extern "C" int scl_launch_zip(scl_program* p, const scl_shape* sh, void* const* 
 }
 
 // ---- Reduce -------------------------------------------------------------------
-extern "C" int scl_launch_reduce(scl_program* p, const scl_shape* sh, void* const* bufs,
+static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* bufs,
                                  const void* extra, size_t extra_bytes, const scl_tuning* tu) {
   if (int st = check_prog(p, {SCL_KIND_REDUCE})) return st;
   if (!sh || !bufs || !bufs[0] || !bufs[1]) return fail(SCL_ERR_ARG, "reduce needs {in, out}");
@@ -313,12 +314,15 @@ extern "C" int scl_launch_reduce(scl_program* p, const scl_shape* sh, void* cons
     // one result per segment, one launch (plus the offsets pre-pass)
     if (!sh->seg_offsets) return fail(SCL_ERR_ARG, "segmented reduce: null seg_offsets");
     uint64_t n_seg = sh->n_segments;
-    // 128 KB tiles for 16-byte vectors: few blocks, each with long streams of loads
-    const uint64_t tile = 32ull * 256 * V;
+    // 128 KB tiles for 16-byte vectors by default: few blocks, each with long
+    // streams of loads (tuning.items = 8: 32 KB tiles)
+    const uint32_t R = (tu && tu->items == 8) ? 8 : 32;
+    const uint64_t tile = (uint64_t)R * 256 * V;
     const uint64_t tiles = (n + tile - 1) / tile + n_seg;
     if (tiles > 0x7fffffffull) return fail(SCL_ERR_ARG, "segmented reduce: too many tiles");
-    CUfunction fn = find_kernel(p, "scl_reduce_seg<32>");
-    if (!fn) return fail(SCL_ERR_LAUNCH, "kernel scl_reduce_seg<32> missing");
+    const std::string kname = "scl_reduce_seg<" + std::to_string(R) + ">";
+    CUfunction fn = find_kernel(p, kname);
+    if (!fn) return fail(SCL_ERR_LAUNCH, "kernel " + kname + " missing");
     auto up = [](size_t b) { return (b + 255) / 256 * 256; };
     const size_t tk = up(n_seg * 4), pa = up(tiles * csz), of = up((n_seg + 1) * 8);
     if (int st = ensure_workspace(p, tk + pa + of + up((n_seg + 1) * 4))) return st;
@@ -365,7 +369,7 @@ extern "C" int scl_launch_reduce(scl_program* p, const scl_shape* sh, void* cons
 }
 
 // ---- Scan ---------------------------------------------------------------------
-extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const* bufs,
+static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bufs,
                                const void* extra, size_t extra_bytes, const scl_tuning* tu) {
   if (int st = check_prog(p, {SCL_KIND_SCAN})) return st;
   if (!sh || !bufs || !bufs[0] || !bufs[1]) return fail(SCL_ERR_ARG, "scan needs {in, out}");
@@ -395,7 +399,7 @@ extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const*
   if (n_seg) {  // segmented: the staged kernel with the default tile shape
     if (!sh->seg_offsets) return fail(SCL_ERR_ARG, "segmented scan: null seg_offsets");
     staged = true;
-    R = 8;
+    R = (tu && tu->items == 16) ? 16 : 8;
     smem = (size_t)R * 256 * V * tsz;
     if (smem + 2048 > rt().smem_optin)
       return fail(SCL_ERR_UNSUPPORTED, "segmented scan: the tile does not fit in shared memory");
@@ -427,7 +431,7 @@ extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const*
                (R == 4 && (minb == 4 || minb == 6)) || (R == 2 && minb == 8))) {
     minb = R == 16 ? 2 : (R == 8 ? 4 : (R == 4 ? 6 : 8));
   }
-  if (n_seg) minb = 6;
+  if (n_seg) minb = R == 16 ? 3 : 6;
   const std::string kname = std::string(staged ? "scl_scan_s<" : "scl_scan_k<") + std::to_string(R) +
                             ", " + std::to_string(minb) + (n_seg ? ", 1>" : ">");
   CUfunction fn = find_kernel(p, kname);
@@ -482,7 +486,7 @@ extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const*
 }
 
 // ---- MapOverlap -----------------------------------------------------------------
-extern "C" int scl_launch_mapoverlap(scl_program* p, const scl_shape* sh, void* const* bufs,
+static int launch_mapoverlap_impl(scl_program* p, const scl_shape* sh, void* const* bufs,
                                      const void* extra, size_t extra_bytes, const scl_tuning* tu) {
   if (int st = check_prog(p, {SCL_KIND_MAPOVERLAP})) return st;
   if (!sh || !bufs || !bufs[0] || !bufs[1]) return fail(SCL_ERR_ARG, "mapoverlap needs {in, out}");
@@ -624,3 +628,106 @@ extern "C" int scl_launch_allpairs(scl_program* p, const scl_shape* sh, void* co
   return launch(fn, grid, dim3(16, 16), staged ? stage : 0, pack);
 }
 
+
+// ---- exported launches: the autotuner in front of each skeleton -------------------
+namespace {
+
+bool overlaps(const void* a, size_t abytes, const void* b, size_t bbytes) {
+  const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+  return a && b && x < y + bbytes && y < x + abytes;
+}
+// extra arguments the user function cannot write through
+bool extras_are_values(const scl_program* p) {
+  for (const Param& e : p->extra)
+    if (e.kind != ParamKind::Value) return false;
+  return true;
+}
+scl_tuning shape(uint32_t workgroup, uint32_t items, uint32_t tile_w, uint32_t tile_h, uint32_t variant) {
+  scl_tuning t{};
+  t.workgroup = workgroup;
+  t.items = items;
+  t.tile_w = tile_w;
+  t.tile_h = tile_h;
+  t.variant = variant;
+  return t;
+}
+
+}  // namespace
+
+extern "C" int scl_launch_map(scl_program* p, const scl_shape* sh, void* const* bufs,
+                              const void* extra, size_t extra_bytes, const scl_tuning* tu) {
+  auto run = [&](const scl_tuning* t) { return launch_map_impl(p, sh, bufs, extra, extra_bytes, t); };
+  if (!p || !sh || !bufs || untuned(tu) == false || p->uses_workitem) return run(tu);
+  const uint64_t n = (p->kind == SCL_KIND_MAP_POINT || p->kind == SCL_KIND_MAP_POINT_VOID) ? sh->rows * sh->cols
+                                                                                          : sh->n;
+  const auto& ts = p->type_sizes;
+  auto sz = [&](size_t i) { return ts.size() > i ? ts[i] : 0; };
+  bool safe = extras_are_values(p);
+  switch (p->kind) {
+    case SCL_KIND_MAP: safe = safe && !overlaps(bufs[0], n * sz(0), bufs[1], n * sz(1)); break;
+    case SCL_KIND_ZIP:
+      safe = safe && !overlaps(bufs[0], n * sz(0), bufs[2], n * sz(2)) &&
+             !overlaps(bufs[1], n * sz(1), bufs[2], n * sz(2));
+      break;
+    case SCL_KIND_MAP_INDEX:
+    case SCL_KIND_MAP_POINT: break;
+    case SCL_KIND_MAP_ADJOINT:
+      safe = safe && !(sh->flags & SCL_SHAPE_ACCUMULATE) && !overlaps(bufs[0], n * sz(0), bufs[2], n * sz(0)) &&
+             !overlaps(bufs[1], n * sz(1), bufs[2], n * sz(0));
+      break;
+    default: safe = false;  // side effects or accumulation: not repeatable
+  }
+  std::vector<scl_tuning> cands;
+  for (uint32_t wg : {128u, 256u, 512u})
+    for (uint32_t items : {1u, 2u, 4u}) cands.push_back(shape(wg, items, 0, 0, 0));
+  return tuned_launch(p, "map", n, tu, safe, cands, run);
+}
+
+extern "C" int scl_launch_reduce(scl_program* p, const scl_shape* sh, void* const* bufs,
+                                 const void* extra, size_t extra_bytes, const scl_tuning* tu) {
+  auto run = [&](const scl_tuning* t) { return launch_reduce_impl(p, sh, bufs, extra, extra_bytes, t); };
+  if (!p || !sh || !bufs || !bufs[0] || !bufs[1] || p->type_sizes.empty()) return run(tu);
+  const size_t tsz = p->type_sizes[0];
+  const uint64_t nout = sh->n_segments ? sh->n_segments : 1;
+  const bool safe = extras_are_values(p) && !overlaps(bufs[0], sh->n * tsz, bufs[1], nout * tsz);
+  std::vector<scl_tuning> cands;
+  if (sh->n_segments) {
+    for (uint32_t r : {8u, 32u}) cands.push_back(shape(0, r, 0, 0, 0));
+    return tuned_launch(p, "reduce_seg", sh->n, tu, safe, cands, run);
+  }
+  for (uint32_t wg : {256u, 512u})
+    for (uint32_t items : {1u, 2u, 4u}) cands.push_back(shape(wg, items, 0, 0, 0));
+  return tuned_launch(p, "reduce", sh->n, tu, safe, cands, run);
+}
+
+extern "C" int scl_launch_scan(scl_program* p, const scl_shape* sh, void* const* bufs,
+                               const void* extra, size_t extra_bytes, const scl_tuning* tu) {
+  auto run = [&](const scl_tuning* t) { return launch_scan_impl(p, sh, bufs, extra, extra_bytes, t); };
+  if (!p || !sh || !bufs || !bufs[0] || !bufs[1] || p->type_sizes.empty()) return run(tu);
+  const size_t bytes = sh->n * p->type_sizes[0];
+  const bool safe = extras_are_values(p) && !overlaps(bufs[0], bytes, bufs[1], bytes);
+  std::vector<scl_tuning> cands;
+  if (sh->n_segments) {
+    cands = {shape(0, 8, 6, 0, 0), shape(0, 16, 3, 0, 0)};
+    return tuned_launch(p, "scan_seg", sh->n, tu, safe, cands, run);
+  }
+  cands = {shape(0, 8, 6, 0, 0), shape(0, 8, 5, 0, 0), shape(0, 16, 3, 0, 0),
+           shape(0, 8, 4, 0, SCL_VARIANT_VECTOR)};
+  return tuned_launch(p, "scan", sh->n, tu, safe, cands, run);
+}
+
+extern "C" int scl_launch_mapoverlap(scl_program* p, const scl_shape* sh, void* const* bufs,
+                                     const void* extra, size_t extra_bytes, const scl_tuning* tu) {
+  auto run = [&](const scl_tuning* t) { return launch_mapoverlap_impl(p, sh, bufs, extra, extra_bytes, t); };
+  if (!p || !sh || !bufs) return run(tu);
+  const bool safe = extras_are_values(p) || [&] {
+    // weights passed as Vector / Matrix arguments are read by the stencil, not written
+    for (const Param& e : p->extra)
+      if (e.kind == ParamKind::Local) return false;
+    return true;
+  }();
+  std::vector<scl_tuning> cands;
+  for (uint32_t v : {SCL_VARIANT_TMA, SCL_VARIANT_LDST})
+    for (uint32_t py : {4u, 8u, 16u}) cands.push_back(shape(0, 0, 0, py, v));
+  return tuned_launch(p, "mapoverlap", sh->rows * sh->cols, tu, safe, cands, run);
+}
