@@ -9,6 +9,7 @@
 #include <string>
 
 #include "Out.h"
+#include "Segments.h"
 #include "Source.h"
 #include "Vector.h"
 #include "detail/Skeleton.h"
@@ -55,6 +56,37 @@ public:
     o.dataOnDeviceModified();
     detail::markModified(args...);
     return o;
+  }
+
+  // One result per vector of `segments` (vectors stored back to back in
+  // `input`), all in one launch; an empty vector yields the identity.
+  template <typename... Args>
+  Vector<T>& segmented(Out<Vector<T>> output, const Vector<T>& input, const Segments& segments,
+                       Args&&... args) const {
+    Vector<T>& o = output.container();
+    ASSERT_MESSAGE(segments.total() <= input.size(), "Reduce::segmented: segments beyond the input");
+    ASSERT((const void*)&o != (const void*)&input);
+    if (o.size() < segments.count()) o.resize(segments.count());
+    if (segments.count() == 0) return o;
+    void* bufs[2];
+    detail::prepareArgs(args...);
+    detail::ArgBlob blob = detail::packArgs(args...);
+    bufs[1] = o.deviceOutputPtr();
+    bufs[0] = input.size() ? (void*)input.devicePtr() : bufs[1];
+    scl_shape sh = detail::makeShape(input.size());
+    sh.seg_offsets = segments.devicePtr();
+    sh.n_segments = segments.count();
+    scl_tuning t = tuning();
+    launched(scl_launch_reduce(_program.get(), &sh, bufs, blob.data(), blob.size(), &t), "Reduce");
+    o.dataOnDeviceModified();
+    detail::markModified(args...);
+    return o;
+  }
+  template <typename... Args>
+  Vector<T> segmented(const Vector<T>& input, const Segments& segments, Args&&... args) const {
+    Vector<T> output;
+    segmented(out(output), input, segments, std::forward<Args>(args)...);
+    return output;
   }
 
   std::string source() const { return _source; }

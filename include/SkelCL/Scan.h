@@ -11,6 +11,7 @@
 #include <string>
 
 #include "Out.h"
+#include "Segments.h"
 #include "Source.h"
 #include "Vector.h"
 #include "detail/Skeleton.h"
@@ -58,6 +59,37 @@ public:
     o.dataOnDeviceModified();
     detail::markModified(args...);
     return o;
+  }
+
+  // One scan per vector of `segments` (vectors stored back to back in
+  // `input`), all in one launch.
+  template <typename... Args>
+  Vector<T>& segmented(Out<Vector<T>> output, const Vector<T>& input, const Segments& segments,
+                       Args&&... args) const {
+    Vector<T>& o = output.container();
+    ASSERT_MESSAGE(segments.total() <= input.size(), "Scan::segmented: segments beyond the input");
+    if ((const void*)&o != (const void*)&input) detail::resizeLike(o, input);
+    if (input.size() == 0 || segments.count() == 0) return o;
+    void* bufs[2];
+    bufs[0] = input.devicePtr();
+    detail::prepareArgs(args...);
+    detail::ArgBlob blob = detail::packArgs(args...);
+    bufs[1] = o.deviceOutputPtr();
+    scl_shape sh = detail::makeShape(input.size());
+    sh.flags = (_inclusive ? SCL_SHAPE_INCLUSIVE : 0u) | (_reverse ? SCL_SHAPE_REVERSE : 0u);
+    sh.seg_offsets = segments.devicePtr();
+    sh.n_segments = segments.count();
+    scl_tuning t = tuning();
+    launched(scl_launch_scan(_program.get(), &sh, bufs, blob.data(), blob.size(), &t), "Scan");
+    o.dataOnDeviceModified();
+    detail::markModified(args...);
+    return o;
+  }
+  template <typename... Args>
+  Vector<T> segmented(const Vector<T>& input, const Segments& segments, Args&&... args) const {
+    Vector<T> output;
+    segmented(out(output), input, segments, std::forward<Args>(args)...);
+    return output;
   }
 
   Scan& setInclusive(bool inclusive) {

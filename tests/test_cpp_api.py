@@ -65,3 +65,19 @@ def test_adjoint_tape_passes_on_gpu(built, tmp_path):
     tail = r.stdout[-6000:] + r.stderr[-2000:]
     assert r.returncode == 0, tail
     assert " 0 failed." in r.stdout, tail
+
+
+def test_extensions_build(built, tmp_path):
+    build_port(tmp_path / "extensions_tests", "extensions_tests.cpp")
+
+
+@pytest.mark.gpu
+def test_extensions_pass_on_gpu(built, tmp_path):
+    """Segmented Scan/Reduce, graph replay and autotuning through the C++ API."""
+    exe = tmp_path / "extensions_tests"
+    build_port(exe, "extensions_tests.cpp")
+    env = dict(os.environ, SKELCL_CACHE_DIR=str(tmp_path))
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=900, cwd=str(tmp_path), env=env)
+    tail = r.stdout[-6000:] + r.stderr[-2000:]
+    assert r.returncode == 0, tail
+    assert " 0 failed." in r.stdout, tail
