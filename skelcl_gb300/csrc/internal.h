@@ -128,6 +128,7 @@ struct scl_program {
   bool tc_eligible = false;                 // AllPairs: zip == x*y, reduce == x+y, id 0, float
   int overlap_range = 0;
   int padding = 0;
+  int stencil_px = 1;                       // MapOverlap: output columns per thread
   std::vector<CUmodule> modules;            // the first holds scl_type_sizes
   std::map<std::string, scl::Kernel> kernels;  // by template name expression
   std::set<std::string> lazy;               // variants compiled on first use

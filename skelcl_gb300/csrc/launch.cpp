@@ -499,7 +499,7 @@ static int launch_mapoverlap_impl(scl_program* p, const scl_shape* sh, void* con
   const bool want_tma = !(tu && tu->variant == SCL_VARIANT_LDST);
   int PY = (tu && tu->tile_h) ? (int)tu->tile_h : 8;  // output rows per thread
   if (PY != 4 && PY != 8 && PY != 16) PY = 8;
-  const int R = p->overlap_range, TW = 32;
+  const int R = p->overlap_range, TW = 32 * p->stencil_px;
   const int xal = tsz <= 16 ? (int)std::max<size_t>(1, 16 / tsz) : 1;
   const int xlead = (R + xal - 1) / xal * xal;
   const int win_w = (xlead + TW + R + xal - 1) / xal * xal;

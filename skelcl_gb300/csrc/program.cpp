@@ -161,7 +161,9 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
     s << "#define SCL_IDENTITY (" << (d->identity && *d->identity ? d->identity : "0") << ")\n";
   if (kind == SCL_KIND_MAPOVERLAP) {
     std::string neutral = d->neutral && *d->neutral ? d->neutral : "0";
-    s << "#define SCL_OVERLAP_RANGE " << d->overlap_range << "\n"
+    p->stencil_px = (d->flags & SCL_PROG_STENCIL_COLS1) ? 1 : 2;
+    s << "#define SCL_PX " << p->stencil_px << "\n"
+      << "#define SCL_OVERLAP_RANGE " << d->overlap_range << "\n"
       << "#define SCL_PADDING " << (d->padding == SCL_PAD_NEAREST ? 1 : 0) << "\n"
       << "#define SCL_NEUTRAL (" << neutral << ")\n"
       << "#define SCL_NEUTRAL_IS_ZERO " << (neutral_is_zero(neutral) ? 1 : 0) << "\n"

@@ -49,26 +49,36 @@ __device__ __forceinline__ void scl_patch_border(SCL_TYPE_0* win, long long x_or
   }
 }
 
+// Each thread computes PY vertically adjacent outputs in each of SCL_PX
+// adjacent columns: with the user loops unrolled, the taps those outputs
+// share are read once.
 template <int PY>
 __device__ __forceinline__ void scl_compute_tile(const SCL_TYPE_0* win, SCL_TYPE_1* out,
                                                  scl_u64 rows, scl_u64 cols, scl_u64 x0,
                                                  scl_u64 y0 SCL_USER_PARAMS) {
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const scl_u64 x = x0 + tx;
-  SCL_TYPE_1 res[PY];
+  SCL_TYPE_1 res[PY][SCL_PX];
 #pragma unroll
   for (int p = 0; p < PY; ++p) {
     const int ly = ty * PY + p;
-    input_matrix_t m;
-    m.data = win + (ly + SCL_R) * SCL_WIN_W + SCL_XLEAD + tx;
-    m.local_row = ly;
-    m.local_column = tx;
-    res[p] = USR_FUNC(m SCL_EXTRA_ARGS);
+#pragma unroll
+    for (int c = 0; c < SCL_PX; ++c) {
+      const int lx = tx * SCL_PX + c;
+      input_matrix_t m;
+      m.data = win + (ly + SCL_R) * SCL_WIN_W + SCL_XLEAD + lx;
+      m.local_row = ly;
+      m.local_column = lx;
+      res[p][c] = USR_FUNC(m SCL_EXTRA_ARGS);
+    }
   }
 #pragma unroll
   for (int p = 0; p < PY; ++p) {
     const scl_u64 y = y0 + ty * PY + p;
-    if (y < rows && x < cols) out[y * cols + x] = res[p];
+#pragma unroll
+    for (int c = 0; c < SCL_PX; ++c) {
+      const scl_u64 x = x0 + (scl_u64)tx * SCL_PX + c;
+      if (y < rows && x < cols) out[y * cols + x] = res[p][c];
+    }
   }
 }
 

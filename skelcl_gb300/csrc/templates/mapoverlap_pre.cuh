@@ -4,7 +4,7 @@
 // getData(m, x, y) reads the staged window at column offset x, row offset y.
 // ---------------------------------------------------------------------------
 #define SCL_R SCL_OVERLAP_RANGE
-#define SCL_TW 32
+#define SCL_TW (32 * SCL_PX)  // tile columns: SCL_PX adjacent columns per thread
 // TMA x coordinates must be multiples of 16 bytes: the window starts
 // SCL_XLEAD >= R elements left of the tile so that x0 - SCL_XLEAD is aligned.
 #define SCL_XALIGN (16 / (int)sizeof(SCL_TYPE_0) > 0 ? 16 / (int)sizeof(SCL_TYPE_0) : 1)
