@@ -55,10 +55,19 @@ enum scl_kind {
    * vector-Jacobian product of the forward function; type_names are the
    * forward's (Tin, Tout / Tl, Tr, Tout).  Launched with scl_launch_map. */
   SCL_KIND_MAP_ADJOINT = 14,    /* Tin  d(Tin x, Tout g, extra...)            */
-  SCL_KIND_ZIP_ADJOINT = 15     /* Tl dl(Tl x, Tr y, Tout g, extra...) = func,
+  SCL_KIND_ZIP_ADJOINT = 15,    /* Tl dl(Tl x, Tr y, Tout g, extra...) = func,
                                    Tr dr(Tl x, Tr y, Tout g, extra...) = func2
                                    (in `source`, or in `source2` if given;
                                    same extra parameters as dl; optional) */
+  /* Fused pairs (no counterpart in the reference, which materialises the
+   * intermediate vector).  `source`/`func` are the first skeleton's, i.e.
+   * the Reduce's / the Scan's, `source2`/`func2` the Zip's / the Map's; extra
+   * arguments: the first function's, then the second's. */
+  SCL_KIND_ZIP_REDUCE = 16,     /* Reduce(Zip(l, r)): types Tl, Tr, T; buffers
+                                   {left, right, out}; launched with
+                                   scl_launch_reduce                        */
+  SCL_KIND_SCAN_MAP = 17        /* Map(Scan(x)): types T, Tout; buffers
+                                   {in, out}; launched with scl_launch_scan  */
 };
 
 /* MapOverlap padding modes (include/SkelCL/detail/Padding.h:47-50). */

@@ -22,7 +22,7 @@ OK, ERR_ARG, ERR_OOM, ERR_COMPILE, ERR_LAUNCH, ERR_TIMEOUT, ERR_CUDA, ERR_NOT_IN
 KIND_MAP, KIND_MAP_VOID, KIND_MAP_INDEX, KIND_MAP_INDEX_VOID = 1, 2, 3, 4
 KIND_MAP_POINT, KIND_MAP_POINT_VOID, KIND_ZIP, KIND_ZIP_VOID = 5, 6, 7, 8
 KIND_REDUCE, KIND_SCAN, KIND_MAPOVERLAP, KIND_ALLPAIRS, KIND_ALLPAIRS_GENERIC = 9, 10, 11, 12, 13
-KIND_MAP_ADJOINT, KIND_ZIP_ADJOINT = 14, 15
+KIND_MAP_ADJOINT, KIND_ZIP_ADJOINT, KIND_ZIP_REDUCE, KIND_SCAN_MAP = 14, 15, 16, 17
 PAD_NEUTRAL, PAD_NEAREST = 0, 1
 SHAPE_INCLUSIVE, SHAPE_REVERSE = 1, 2
 SHAPE_ACCUMULATE, SHAPE_ACCUMULATE_RIGHT, SHAPE_TRANS_LEFT, SHAPE_TRANS_RIGHT = 4, 8, 16, 32
@@ -298,7 +298,8 @@ _LAUNCH = {KIND_MAP: "scl_launch_map", KIND_MAP_VOID: "scl_launch_map",
            KIND_REDUCE: "scl_launch_reduce", KIND_SCAN: "scl_launch_scan",
            KIND_MAPOVERLAP: "scl_launch_mapoverlap", KIND_ALLPAIRS: "scl_launch_allpairs",
            KIND_ALLPAIRS_GENERIC: "scl_launch_allpairs",
-           KIND_MAP_ADJOINT: "scl_launch_map", KIND_ZIP_ADJOINT: "scl_launch_map"}
+           KIND_MAP_ADJOINT: "scl_launch_map", KIND_ZIP_ADJOINT: "scl_launch_map",
+           KIND_ZIP_REDUCE: "scl_launch_reduce", KIND_SCAN_MAP: "scl_launch_scan"}
 
 
 class Program:

@@ -300,9 +300,13 @@ extern "C" int scl_launch_zip(scl_program* p, const scl_shape* sh, void* const* 
 }
 
 // ---- Reduce -------------------------------------------------------------------
+static int launch_zipreduce(scl_program* p, const scl_shape* sh, void* const* bufs,
+                            const void* extra, size_t extra_bytes, const scl_tuning* tu);
+
 static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* bufs,
                                  const void* extra, size_t extra_bytes, const scl_tuning* tu) {
-  if (int st = check_prog(p, {SCL_KIND_REDUCE})) return st;
+  if (int st = check_prog(p, {SCL_KIND_REDUCE, SCL_KIND_ZIP_REDUCE})) return st;
+  if (p->kind == SCL_KIND_ZIP_REDUCE) return launch_zipreduce(p, sh, bufs, extra, extra_bytes, tu);
   if (!sh || !bufs || !bufs[0] || !bufs[1]) return fail(SCL_ERR_ARG, "reduce needs {in, out}");
   void* in = bufs[0];
   void* out = bufs[1];
@@ -368,10 +372,49 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
   return launch(fn, dim3((unsigned)g), dim3(wg), 0, pack);
 }
 
+// Reduce(Zip(left, right)) in one pass: buffers {left, right, out}.
+static int launch_zipreduce(scl_program* p, const scl_shape* sh, void* const* bufs,
+                            const void* extra, size_t extra_bytes, const scl_tuning* tu) {
+  if (!sh || !bufs || !bufs[0] || !bufs[1] || !bufs[2])
+    return fail(SCL_ERR_ARG, "fused zip-reduce needs {left, right, out}");
+  if (sh->n_segments) return fail(SCL_ERR_UNSUPPORTED, "fused zip-reduce: no segmented form");
+  void* l = bufs[0];
+  void* r = bufs[1];
+  void* out = bufs[2];
+  uint64_t n = sh->n;
+  const size_t s0 = p->type_sizes[0], s1 = p->type_sizes[1], tsz = p->type_sizes[2];
+  const size_t csz = p->carry_size ? p->carry_size : tsz;
+  const int V = vec_width(s0, s1);
+  int aligned = (aligned16(l) && aligned16(r)) ? 1 : 0;
+  uint32_t items = (tu && tu->items) ? tu->items : 4;
+  if (items != 1 && items != 2 && items != 4) items = 4;
+  const std::string kname = "scl_zipreduce_k<" + std::to_string(items) + ">";
+  CUfunction fn = find_kernel(p, kname);
+  if (!fn) return fail(SCL_ERR_LAUNCH, "kernel " + kname + " missing");
+  uint32_t wg = pick_block(tu, 256);
+  wg = (wg + 31) / 32 * 32;
+  const int maxb = max_resident_blocks(fn, (int)wg, 0);
+  uint64_t units = aligned ? n / V : n;
+  uint64_t g = units == 0 ? 1 : (units + wg - 1) / wg;
+  if (g > (uint64_t)maxb) g = (uint64_t)maxb;
+  if (g < 1) g = 1;
+  const size_t part_off = 256;
+  if (int st = ensure_workspace(p, part_off + g * csz)) return st;
+  void* partials = (char*)p->ws.ptr + part_off;
+  void* ticket = p->ws.ptr;
+  unsigned int* err = rt().dev_err;
+  ArgPack pack;
+  pack.ptrs = {&l, &r, &out, &n, &aligned, &partials, &ticket, &err};
+  if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
+    return st;
+  p->last_variant = SCL_VARIANT_VECTOR;
+  return launch(fn, dim3((unsigned)g), dim3(wg), 0, pack);
+}
+
 // ---- Scan ---------------------------------------------------------------------
 static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bufs,
                                const void* extra, size_t extra_bytes, const scl_tuning* tu) {
-  if (int st = check_prog(p, {SCL_KIND_SCAN})) return st;
+  if (int st = check_prog(p, {SCL_KIND_SCAN, SCL_KIND_SCAN_MAP})) return st;
   if (!sh || !bufs || !bufs[0] || !bufs[1]) return fail(SCL_ERR_ARG, "scan needs {in, out}");
   void* in = bufs[0];
   void* out = bufs[1];
@@ -388,10 +431,12 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   // default: the shared-memory staged kernel (measured 5.7 TB/s on int32 2^28
   // against 5.1 for the tile held in registers); SCL_VARIANT_VECTOR selects
   // the register kernel
-  bool staged = !(tu && tu->variant == SCL_VARIANT_VECTOR);
+  bool staged = !(tu && tu->variant == SCL_VARIANT_VECTOR) || p->kind == SCL_KIND_SCAN_MAP;
   if (staged && R == 2) R = 4;
   size_t smem = staged ? (size_t)R * 256 * V * tsz : 0;
   if (staged && smem + 2048 > rt().smem_optin) {
+    if (p->kind == SCL_KIND_SCAN_MAP)
+      return fail(SCL_ERR_UNSUPPORTED, "fused scan-map: the tile does not fit in shared memory");
     staged = false;
     smem = 0;
   }
@@ -687,6 +732,16 @@ extern "C" int scl_launch_reduce(scl_program* p, const scl_shape* sh, void* cons
                                  const void* extra, size_t extra_bytes, const scl_tuning* tu) {
   auto run = [&](const scl_tuning* t) { return launch_reduce_impl(p, sh, bufs, extra, extra_bytes, t); };
   if (!p || !sh || !bufs || !bufs[0] || !bufs[1] || p->type_sizes.empty()) return run(tu);
+  if (p->kind == SCL_KIND_ZIP_REDUCE) {
+    if (!bufs[2] || p->type_sizes.size() < 3) return run(tu);
+    const bool safe = extras_are_values(p) &&
+                      !overlaps(bufs[0], sh->n * p->type_sizes[0], bufs[2], p->type_sizes[2]) &&
+                      !overlaps(bufs[1], sh->n * p->type_sizes[1], bufs[2], p->type_sizes[2]);
+    std::vector<scl_tuning> cands;
+    for (uint32_t wg : {256u, 512u})
+      for (uint32_t items : {1u, 2u, 4u}) cands.push_back(shape(wg, items, 0, 0, 0));
+    return tuned_launch(p, "zipreduce", sh->n, tu, safe, cands, run);
+  }
   const size_t tsz = p->type_sizes[0];
   const uint64_t nout = sh->n_segments ? sh->n_segments : 1;
   const bool safe = extras_are_values(p) && !overlaps(bufs[0], sh->n * tsz, bufs[1], nout * tsz);

@@ -131,6 +131,20 @@ bool neutral_is_zero(const std::string& s) {
   return end && *end == '\0' && v == 0.0;
 }
 
+// Float folds (Reduce, Scan and their fused forms) carry across blocks in FP64.
+bool wants_f64_carry(const scl_program_desc* d) {
+  if (d->flags & SCL_PROG_NO_F64_CARRY) return false;
+  int t = -1;  // the folded type
+  if (d->kind == SCL_KIND_REDUCE || d->kind == SCL_KIND_SCAN || d->kind == SCL_KIND_SCAN_MAP) t = 0;
+  if (d->kind == SCL_KIND_ZIP_REDUCE) t = 2;
+  return t >= 0 && d->n_types > t && d->type_names[t] && std::string(d->type_names[t]) == "float";
+}
+
+bool folds(int kind) {
+  return kind == SCL_KIND_REDUCE || kind == SCL_KIND_SCAN || kind == SCL_KIND_ZIP_REDUCE ||
+         kind == SCL_KIND_SCAN_MAP;
+}
+
 struct Assembly {
   std::string source;
   std::vector<std::string> kernels;  // name expressions compiled at construction
@@ -157,7 +171,7 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
   if (kind == SCL_KIND_MAP_INDEX || kind == SCL_KIND_MAP_INDEX_VOID)
     s << "typedef size_t Index;\n";
   if (point) s << "typedef struct { size_t x; size_t y; } IndexPoint;\n";
-  if (kind == SCL_KIND_REDUCE || kind == SCL_KIND_SCAN || kind == SCL_KIND_ALLPAIRS)
+  if (folds(kind) || kind == SCL_KIND_ALLPAIRS)
     s << "#define SCL_IDENTITY (" << (d->identity && *d->identity ? d->identity : "0") << ")\n";
   if (kind == SCL_KIND_MAPOVERLAP) {
     std::string neutral = d->neutral && *d->neutral ? d->neutral : "0";
@@ -177,7 +191,42 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
   p->extra.clear();
   p->n_reduce_extra = 0;
   std::string zip_args, reduce_args;
-  if (kind == SCL_KIND_ALLPAIRS) {
+  if (kind == SCL_KIND_ZIP_REDUCE || kind == SCL_KIND_SCAN_MAP) {
+    // the folding function becomes SCL_FUNC (with its FP64 twin), the second
+    // USR_ZIP / USR_MAP; extras: the fold's, then the second function's
+    const std::string func2 = d->func2 ? d->func2 : "func";
+    const std::string src2 = strip_opencl_pragmas(d->source2 ? d->source2 : "");
+    const char* second = kind == SCL_KIND_ZIP_REDUCE ? "USR_ZIP" : "USR_MAP";
+    const size_t arity2 = kind == SCL_KIND_ZIP_REDUCE ? 2 : 1;
+    FuncSig fs, ss;
+    if (!parse_function(src, func, &fs, err)) { *err = "fold source: " + *err; return SCL_ERR_COMPILE; }
+    if (!parse_function(src2, func2, &ss, err)) { *err = "second source: " + *err; return SCL_ERR_COMPILE; }
+    if (fs.params.size() < 2 || ss.params.size() < arity2) {
+      *err = "fused skeleton: the fold takes two parameters, the second function " + std::to_string(arity2);
+      return SCL_ERR_COMPILE;
+    }
+    std::vector<Param> fx(fs.params.begin() + 2, fs.params.end());
+    std::vector<Param> sx(ss.params.begin() + arity2, ss.params.end());
+    const std::string renamed = rename_identifier(src, func, "SCL_FUNC");
+    s << "// ---- fold user source\n" << renamed << "\n";
+    s << "// ---- second user source\n" << rename_identifier(src2, func2, second) << "\n";
+    if (want_f64) {
+      FuncSig rsig;
+      std::string e2;
+      if (parse_function(renamed, "SCL_FUNC", &rsig, &e2)) {
+        std::string def = renamed.substr(rsig.def_begin, rsig.def_end - rsig.def_begin);
+        def = rename_identifier(def, "float", "double");
+        def = rename_identifier(def, "SCL_FUNC", "SCL_FUNC_C");
+        s << "// ---- FP64 twin for carries\n" << def << "\n";
+      }
+    }
+    append_extra(fx, 0, &em, &reduce_args);
+    append_extra(sx, fx.size(), &em, &zip_args);
+    p->extra = fx;
+    p->extra.insert(p->extra.end(), sx.begin(), sx.end());
+    p->n_reduce_extra = fx.size();
+    p->uses_workitem = false;
+  } else if (kind == SCL_KIND_ALLPAIRS) {
     const std::string func2 = d->func2 ? d->func2 : "func";
     const std::string src2 = strip_opencl_pragmas(d->source2 ? d->source2 : "");
     FuncSig rs, zs;
@@ -267,9 +316,15 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
     << "#define SCL_EXTRA_ARGS " << em.args << "\n"
     << "#define SCL_REDUCE_ARGS " << reduce_args << "\n"
     << "#define SCL_ZIP_ARGS " << zip_args << "\n";
-  if (kind == SCL_KIND_REDUCE || kind == SCL_KIND_SCAN) {
+  // the fold's own extra arguments, and the second function's (fused kinds)
+  if (kind == SCL_KIND_ZIP_REDUCE || kind == SCL_KIND_SCAN_MAP)
+    s << "#define SCL_OP_ARGS SCL_REDUCE_ARGS\n#define SCL_SECOND_ARGS SCL_ZIP_ARGS\n";
+  else
+    s << "#define SCL_OP_ARGS SCL_EXTRA_ARGS\n#define SCL_SECOND_ARGS\n";
+  if (folds(kind)) {
     if (want_f64) s << "typedef double SCL_CARRY_T;\n";
-    else s << "typedef SCL_TYPE_0 SCL_CARRY_T;\n#define SCL_FUNC_C SCL_FUNC\n";
+    else s << "typedef SCL_TYPE_" << (kind == SCL_KIND_ZIP_REDUCE ? 2 : 0)
+           << " SCL_CARRY_T;\n#define SCL_FUNC_C SCL_FUNC\n";
   }
   s << "// ---- skeleton template\n";
   switch (kind) {
@@ -293,6 +348,16 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
                    "scl_scan_s<8, 5>", "scl_scan_s<8, 4>", "scl_scan_s<4, 8>",
                    "scl_scan_s<16, 3>", "scl_scan_s<8, 6, 1>", "scl_scan_s<16, 3, 1>"};
       break;
+    case SCL_KIND_ZIP_REDUCE:
+      s << scl_tpl_reduce;
+      out->kernels = {"scl_zipreduce_k<1>", "scl_zipreduce_k<2>", "scl_zipreduce_k<4>"};
+      break;
+    case SCL_KIND_SCAN_MAP:
+      s << scl_tpl_reduce << "\n" << scl_tpl_scan;
+      out->kernels = {"scl_scan_s<8, 6>"};
+      out->lazy = {"scl_scan_s<8, 5>", "scl_scan_s<8, 4>", "scl_scan_s<4, 8>", "scl_scan_s<16, 3>",
+                   "scl_scan_s<8, 6, 1>", "scl_scan_s<16, 3, 1>"};
+      break;
     case SCL_KIND_MAPOVERLAP:
       s << scl_tpl_mapoverlap;
       out->kernels = {"scl_mapoverlap_tma<8>"};
@@ -315,8 +380,9 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
   s << "\nextern \"C\" __device__ const unsigned int scl_type_sizes[5] = {";
   for (int i = 0; i < 3; ++i)
     s << (i < d->n_types ? "(unsigned int)sizeof(SCL_TYPE_" + std::to_string(i) + ")" : std::string("0u")) << ", ";
-  s << ((kind == SCL_KIND_REDUCE || kind == SCL_KIND_SCAN) ? "(unsigned int)sizeof(SCL_CARRY_T)" : "0u")
-    << ", " << (kind == SCL_KIND_SCAN ? "(unsigned int)scl_status_mode<SCL_CARRY_T>::value" : "0u")
+  s << (folds(kind) ? "(unsigned int)sizeof(SCL_CARRY_T)" : "0u")
+    << ", " << ((kind == SCL_KIND_SCAN || kind == SCL_KIND_SCAN_MAP)
+                    ? "(unsigned int)scl_status_mode<SCL_CARRY_T>::value" : "0u")
     << "};\n";
   out->source = s.str();
   return SCL_OK;
@@ -559,9 +625,7 @@ extern "C" int scl_program_build(const scl_program_desc* desc, scl_program** out
   p->padding = desc->padding;
   for (int i = 0; i < desc->n_types; ++i) p->type_names.push_back(desc->type_names[i]);
 
-  bool want_f64 = (desc->kind == SCL_KIND_REDUCE || desc->kind == SCL_KIND_SCAN) &&
-                  desc->n_types >= 1 && std::string(desc->type_names[0]) == "float" &&
-                  !(desc->flags & SCL_PROG_NO_F64_CARRY);
+  bool want_f64 = wants_f64_carry(desc);
   std::string cubin, nvlog, err;
   std::map<std::string, std::string> lowered;
   Assembly a;
@@ -613,10 +677,7 @@ extern "C" int scl_program_compile(const scl_program_desc* desc, char* log, size
   if (!desc) return fail(SCL_ERR_ARG, "scl_program_compile: null desc");
   scl_program tmp;
   tmp.kind = desc->kind;
-  bool want_f64 = (desc->kind == SCL_KIND_REDUCE || desc->kind == SCL_KIND_SCAN) &&
-                  desc->n_types >= 1 && desc->type_names[0] &&
-                  std::string(desc->type_names[0]) == "float" &&
-                  !(desc->flags & SCL_PROG_NO_F64_CARRY);
+  bool want_f64 = wants_f64_carry(desc);
   std::string err, nvlog, cubin;
   std::map<std::string, std::string> lowered;
   for (int attempt = 0; attempt < 2; ++attempt) {

@@ -86,8 +86,12 @@ __device__ __forceinline__ void scl_st_cg(T* p, const T& v) {
   }
 }
 
-#if SCL_KIND == 9
+#if SCL_KIND == 9 || SCL_KIND == 16
+#if SCL_KIND == 16
+typedef SCL_TYPE_2 scl_T;  // the zipped element type folded by the Reduce
+#else
 typedef SCL_TYPE_0 scl_T;
+#endif
 typedef SCL_CARRY_T scl_C;
 
 // Fold (have, value) pairs across a warp; lane 0 ends with the warp's fold.
@@ -97,7 +101,7 @@ __device__ __forceinline__ void scl_warp_fold(bool& have, scl_C& c SCL_USER_PARA
     scl_C o = scl_shfl_down(c, off);
     bool oh = __shfl_down_sync(0xffffffffu, have ? 1 : 0, off) != 0;
     if ((threadIdx.x & 31) + off < 32 && oh) {
-      c = have ? (scl_C)SCL_FUNC_C(c, o SCL_EXTRA_ARGS) : o;
+      c = have ? (scl_C)SCL_FUNC_C(c, o SCL_OP_ARGS) : o;
       have = true;
     }
   }
@@ -123,6 +127,7 @@ __device__ __forceinline__ void scl_block_fold(bool& have, scl_C& c SCL_USER_PAR
   __syncthreads();
 }
 
+#if SCL_KIND == 9
 template <int U>
 __global__ void scl_reduce_k(const scl_T* in, scl_T* out, scl_u64 n, int aligned,
                              scl_C* partials, unsigned int* ticket,
@@ -142,7 +147,7 @@ __global__ void scl_reduce_k(const scl_T* in, scl_T* out, scl_u64 n, int aligned
     scl_pack<scl_T, V> p = scl_load<scl_T, V>(in + j * V);
     acc = p.v[0];
 #pragma unroll
-    for (int e = 1; e < V; ++e) acc = SCL_FUNC(acc, p.v[e] SCL_EXTRA_ARGS);
+    for (int e = 1; e < V; ++e) acc = SCL_FUNC(acc, p.v[e] SCL_OP_ARGS);
     have = true;
     j += nth;
   }
@@ -158,12 +163,12 @@ __global__ void scl_reduce_k(const scl_T* in, scl_T* out, scl_u64 n, int aligned
       const scl_u64 k = j + (scl_u64)u * nth;
       if (k < nvec) {
 #pragma unroll
-        for (int e = 0; e < V; ++e) acc = SCL_FUNC(acc, a[u].v[e] SCL_EXTRA_ARGS);
+        for (int e = 0; e < V; ++e) acc = SCL_FUNC(acc, a[u].v[e] SCL_OP_ARGS);
       }
     }
   }
   for (scl_u64 i = nvec * V + tid; i < n; i += nth) {
-    acc = have ? SCL_FUNC(acc, in[i] SCL_EXTRA_ARGS) : in[i];
+    acc = have ? SCL_FUNC(acc, in[i] SCL_OP_ARGS) : in[i];
     have = true;
   }
   scl_C c;
@@ -184,7 +189,7 @@ __global__ void scl_reduce_k(const scl_T* in, scl_T* out, scl_u64 n, int aligned
   have = false;
   for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
     scl_C v = scl_ld_cg(&partials[b]);
-    c = have ? (scl_C)SCL_FUNC_C(c, v SCL_EXTRA_ARGS) : v;
+    c = have ? (scl_C)SCL_FUNC_C(c, v SCL_OP_ARGS) : v;
     have = true;
   }
   scl_block_fold(have, c SCL_EXTRA_ARGS);
@@ -252,7 +257,7 @@ scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
       for (int r = 0; r < G; ++r)
 #pragma unroll
         for (int e = 0; e < V; ++e) {
-          acc = have ? SCL_FUNC(acc, a[r].v[e] SCL_EXTRA_ARGS) : a[r].v[e];
+          acc = have ? SCL_FUNC(acc, a[r].v[e] SCL_OP_ARGS) : a[r].v[e];
           have = true;
         }
     }
@@ -267,19 +272,19 @@ scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
       bend = h + (end - h) / V * V;
     }
     for (scl_u64 i = begin + threadIdx.x; i < h; i += B) {
-      acc = have ? SCL_FUNC(acc, src[i] SCL_EXTRA_ARGS) : src[i];
+      acc = have ? SCL_FUNC(acc, src[i] SCL_OP_ARGS) : src[i];
       have = true;
     }
     for (scl_u64 i = h + (scl_u64)threadIdx.x * V; i < bend; i += (scl_u64)B * V) {
       scl_pack<scl_T, V> a = scl_load<scl_T, V>(src + i);
 #pragma unroll
       for (int e = 0; e < V; ++e) {
-        acc = have ? SCL_FUNC(acc, a.v[e] SCL_EXTRA_ARGS) : a.v[e];
+        acc = have ? SCL_FUNC(acc, a.v[e] SCL_OP_ARGS) : a.v[e];
         have = true;
       }
     }
     for (scl_u64 i = (bend > h ? bend : h) + threadIdx.x; i < end; i += B) {
-      acc = have ? SCL_FUNC(acc, src[i] SCL_EXTRA_ARGS) : src[i];
+      acc = have ? SCL_FUNC(acc, src[i] SCL_OP_ARGS) : src[i];
       have = true;
     }
   }
@@ -302,7 +307,7 @@ scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
   have = false;
   for (unsigned int b = threadIdx.x; b < count; b += B) {
     scl_C v = scl_ld_cg(&partials[first + b]);
-    c = have ? (scl_C)SCL_FUNC_C(c, v SCL_EXTRA_ARGS) : v;
+    c = have ? (scl_C)SCL_FUNC_C(c, v SCL_OP_ARGS) : v;
     have = true;
   }
   scl_block_fold(have, c SCL_EXTRA_ARGS);
@@ -311,4 +316,82 @@ scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
     tickets[sg] = 0u;
   }
 }
+#endif  // SCL_KIND == 9
+
+#if SCL_KIND == 16
+// Fused Zip -> Reduce (no counterpart in the reference, which materialises
+// the zipped vector): out[0] = fold over i of USR_ZIP(left[i], right[i]),
+// in one pass over both inputs with the single-pass reduce above (per-thread
+// fold, FP64 carries for float, last-block combine).  Extra arguments: the
+// Reduce's first, then the Zip's.
+template <int U>
+__global__ void scl_zipreduce_k(const SCL_TYPE_0* left, const SCL_TYPE_1* right, scl_T* out,
+                                scl_u64 n, int aligned, scl_C* partials, unsigned int* ticket,
+                                unsigned int* err SCL_EXTRA_PARAMS) {
+  SCL_EXTRA_SETUP
+  constexpr int V = scl_vec_width<sizeof(SCL_TYPE_0), sizeof(SCL_TYPE_1)>::value;
+  const scl_u64 tid = SCL_TID(), nth = SCL_NTH();
+  if (n == 0) {
+    if (tid == 0) out[0] = (scl_T)(SCL_IDENTITY);
+    return;
+  }
+  const scl_u64 nvec = aligned ? n / V : 0;
+  bool have = false;
+  scl_T acc;
+  for (scl_u64 j = tid; j < nvec; j += nth * U) {
+    scl_pack<SCL_TYPE_0, V> a[U];
+    scl_pack<SCL_TYPE_1, V> b[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const scl_u64 k = j + (scl_u64)u * nth;
+      if (k < nvec) {
+        a[u] = scl_load<SCL_TYPE_0, V>(left + k * V);
+        b[u] = scl_load<SCL_TYPE_1, V>(right + k * V);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const scl_u64 k = j + (scl_u64)u * nth;
+      if (k < nvec) {
+#pragma unroll
+        for (int e = 0; e < V; ++e) {
+          const scl_T z = USR_ZIP(a[u].v[e], b[u].v[e] SCL_SECOND_ARGS);
+          acc = have ? SCL_FUNC(acc, z SCL_OP_ARGS) : z;
+          have = true;
+        }
+      }
+    }
+  }
+  for (scl_u64 i = nvec * V + tid; i < n; i += nth) {
+    const scl_T z = USR_ZIP(left[i], right[i] SCL_SECOND_ARGS);
+    acc = have ? SCL_FUNC(acc, z SCL_OP_ARGS) : z;
+    have = true;
+  }
+  scl_C c;
+  if (have) c = (scl_C)acc;
+  scl_block_fold(have, c SCL_EXTRA_ARGS);
+
+  __shared__ int s_last;
+  if (threadIdx.x == 0) {
+    scl_st_cg(&partials[blockIdx.x], c);  // every block holds at least one element
+    __threadfence();
+    const unsigned int t = atomicAdd(ticket, 1u);
+    s_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  have = false;
+  for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+    scl_C v = scl_ld_cg(&partials[b]);
+    c = have ? (scl_C)SCL_FUNC_C(c, v SCL_OP_ARGS) : v;
+    have = true;
+  }
+  scl_block_fold(have, c SCL_EXTRA_ARGS);
+  if (threadIdx.x == 0) {
+    out[0] = (scl_T)c;
+    *ticket = 0u;
+  }
+}
+#endif  // SCL_KIND == 16
 #endif

@@ -36,9 +36,19 @@
 //   mode 0, other carries   : flag word (release/acquire) + separate values
 // ---------------------------------------------------------------------------
 
-#if SCL_KIND == 10
+#if SCL_KIND == 10 || SCL_KIND == 17
 typedef SCL_TYPE_0 scl_T;
 typedef SCL_CARRY_T scl_C;
+#if SCL_KIND == 17
+// Fused Scan -> Map (no counterpart in the reference, which materialises the
+// scanned vector): the staged kernel stores USR_MAP(scan value) instead of
+// the scan value.  Extra arguments: the Scan's first, then the Map's.
+typedef SCL_TYPE_1 scl_O;
+#define SCL_EPILOGUE(v) USR_MAP(v SCL_SECOND_ARGS)
+#else
+typedef scl_T scl_O;
+#define SCL_EPILOGUE(v) (v)
+#endif
 
 #define SCL_SCAN_B 256
 #define SCL_SCAN_W 8
@@ -93,7 +103,7 @@ __device__ __forceinline__ T scl_warp_incl(T v SCL_USER_PARAMS) {
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
     T o = scl_shfl_up(v, off);
-    if (lane >= off) v = SCL_FUNC(o, v SCL_EXTRA_ARGS);
+    if (lane >= off) v = SCL_FUNC(o, v SCL_OP_ARGS);
   }
   return v;
 }
@@ -192,7 +202,7 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
 #pragma unroll
   for (int r = 0; r < R; ++r) {
 #pragma unroll
-    for (int e = 1; e < V; ++e) x[r][e] = SCL_FUNC(x[r][e - 1], x[r][e] SCL_EXTRA_ARGS);
+    for (int e = 1; e < V; ++e) x[r][e] = SCL_FUNC(x[r][e - 1], x[r][e] SCL_OP_ARGS);
     wincl[r] = scl_warp_incl(x[r][V - 1] SCL_EXTRA_ARGS);
     if (lane == 31) s_wsum[r * W + warp] = wincl[r];
   }
@@ -209,9 +219,9 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
       scl_T vi = scl_warp_incl(v SCL_EXTRA_ARGS);
       scl_T ve = scl_shfl_up(vi, 1);
       if (lane == 0) ve = ident;
-      if (q < R * W) s_wsum[q] = SCL_FUNC(carry, ve SCL_EXTRA_ARGS);
+      if (q < R * W) s_wsum[q] = SCL_FUNC(carry, ve SCL_OP_ARGS);
       scl_T total = scl_shfl_idx(vi, 31);
-      carry = SCL_FUNC(carry, total SCL_EXTRA_ARGS);
+      carry = SCL_FUNC(carry, total SCL_OP_ARGS);
     }
     const scl_C aggc = (scl_C)carry;
     scl_C prefix = (scl_C)ident;
@@ -238,15 +248,15 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
           scl_C o = scl_shfl_down(v, off);
-          if (lane + off < 32) v = (scl_C)SCL_FUNC_C(o, v SCL_EXTRA_ARGS);
+          if (lane + off < 32) v = (scl_C)SCL_FUNC_C(o, v SCL_OP_ARGS);
         }
         const scl_C window = scl_shfl_idx(v, 0);
-        running = (scl_C)SCL_FUNC_C(window, running SCL_EXTRA_ARGS);
+        running = (scl_C)SCL_FUNC_C(window, running SCL_OP_ARGS);
         if (pmask) break;
         pred -= 32;
       }
       prefix = running;
-      if (lane == 0) scl_publish(st, tile, true, (scl_C)SCL_FUNC_C(prefix, aggc SCL_EXTRA_ARGS));
+      if (lane == 0) scl_publish(st, tile, true, (scl_C)SCL_FUNC_C(prefix, aggc SCL_OP_ARGS));
     }
     if (lane == 0) s_prefix = prefix;
   }
@@ -258,14 +268,14 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
   for (int r = 0; r < R; ++r) {
     scl_T lane_excl = scl_shfl_up(wincl[r], 1);
     if (lane == 0) lane_excl = ident;
-    const scl_T pre = SCL_FUNC(SCL_FUNC(tile_carry, s_wsum[r * W + warp] SCL_EXTRA_ARGS),
-                               lane_excl SCL_EXTRA_ARGS);
+    const scl_T pre = SCL_FUNC(SCL_FUNC(tile_carry, s_wsum[r * W + warp] SCL_OP_ARGS),
+                               lane_excl SCL_OP_ARGS);
     if (inclusive) {
 #pragma unroll
-      for (int e = 0; e < V; ++e) x[r][e] = SCL_FUNC(pre, x[r][e] SCL_EXTRA_ARGS);
+      for (int e = 0; e < V; ++e) x[r][e] = SCL_FUNC(pre, x[r][e] SCL_OP_ARGS);
     } else {
 #pragma unroll
-      for (int e = V - 1; e > 0; --e) x[r][e] = SCL_FUNC(pre, x[r][e - 1] SCL_EXTRA_ARGS);
+      for (int e = V - 1; e > 0; --e) x[r][e] = SCL_FUNC(pre, x[r][e - 1] SCL_OP_ARGS);
       x[r][0] = pre;
     }
   }
@@ -338,7 +348,7 @@ __device__ __forceinline__ bool scl_mbar_wait(unsigned int bar_s, unsigned int s
 // upper bound) return at once.
 template <int R, int MINB, int SEG = 0>
 __global__ void __launch_bounds__(SCL_SCAN_B, MINB)
-scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int aligned,
+scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int aligned,
            unsigned int* tile_counter, scl_scan_status st, unsigned int spin_limit,
            unsigned int* err, const scl_u64* seg_off, const unsigned int* tile_start,
            scl_u64 n_seg SCL_EXTRA_PARAMS) {
@@ -486,7 +496,7 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
       }
     }
 #pragma unroll
-    for (int e = 1; e < V; ++e) p.v[e] = SCL_FUNC(p.v[e - 1], p.v[e] SCL_EXTRA_ARGS);
+    for (int e = 1; e < V; ++e) p.v[e] = SCL_FUNC(p.v[e - 1], p.v[e] SCL_OP_ARGS);
     scl_store<scl_T, V>(ts + pos, p);
     wincl[r] = scl_warp_incl(p.v[V - 1] SCL_EXTRA_ARGS);
     if (lane == 31) s_wsum[r * W + warp] = wincl[r];
@@ -503,9 +513,9 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
       scl_T vi = scl_warp_incl(v SCL_EXTRA_ARGS);
       scl_T ve = scl_shfl_up(vi, 1);
       if (lane == 0) ve = ident;
-      if (q < R * W) s_wsum[q] = SCL_FUNC(carry, ve SCL_EXTRA_ARGS);
+      if (q < R * W) s_wsum[q] = SCL_FUNC(carry, ve SCL_OP_ARGS);
       scl_T total = scl_shfl_idx(vi, 31);
-      carry = SCL_FUNC(carry, total SCL_EXTRA_ARGS);
+      carry = SCL_FUNC(carry, total SCL_OP_ARGS);
     }
     const scl_C aggc = (scl_C)carry;
     scl_C prefix = (scl_C)ident;
@@ -531,15 +541,15 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
           scl_C o = scl_shfl_down(v, off);
-          if (lane + off < 32) v = (scl_C)SCL_FUNC_C(o, v SCL_EXTRA_ARGS);
+          if (lane + off < 32) v = (scl_C)SCL_FUNC_C(o, v SCL_OP_ARGS);
         }
         const scl_C window = scl_shfl_idx(v, 0);
-        running = (scl_C)SCL_FUNC_C(window, running SCL_EXTRA_ARGS);
+        running = (scl_C)SCL_FUNC_C(window, running SCL_OP_ARGS);
         if (pmask) break;
         pred -= 32;
       }
       prefix = running;
-      if (lane == 0) scl_publish(st, tile, true, (scl_C)SCL_FUNC_C(prefix, aggc SCL_EXTRA_ARGS));
+      if (lane == 0) scl_publish(st, tile, true, (scl_C)SCL_FUNC_C(prefix, aggc SCL_OP_ARGS));
     }
     if (lane == 0) s_prefix = prefix;
   }
@@ -547,7 +557,9 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
 
   // ---- outputs: 16-byte stores for whole slots when `out` shares the grid
   const scl_T tile_carry = (scl_T)s_prefix;
-  const bool ovec = full && (((scl_u64)out + (scl_u64)(tile_lo * (long long)sizeof(scl_T))) & 15u) == 0;
+  // (whole-slot stores need the output elements the size of the scanned ones)
+  const bool ovec = sizeof(scl_O) == sizeof(scl_T) && full &&
+                    (((scl_u64)out + (scl_u64)(tile_lo * (long long)sizeof(scl_O))) & 15u) == 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int q = r * B + threadIdx.x;
@@ -555,16 +567,16 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
     scl_pack<scl_T, V> p = scl_load<scl_T, V>(ts + pos);
     scl_T lane_excl = scl_shfl_up(wincl[r], 1);
     if (lane == 0) lane_excl = ident;
-    const scl_T pre = SCL_FUNC(SCL_FUNC(tile_carry, s_wsum[r * W + warp] SCL_EXTRA_ARGS),
-                               lane_excl SCL_EXTRA_ARGS);
+    const scl_T pre = SCL_FUNC(SCL_FUNC(tile_carry, s_wsum[r * W + warp] SCL_OP_ARGS),
+                               lane_excl SCL_OP_ARGS);
     scl_pack<scl_T, V> o;  // logical order
     if (inclusive) {
 #pragma unroll
-      for (int e = 0; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e] SCL_EXTRA_ARGS);
+      for (int e = 0; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e] SCL_OP_ARGS);
     } else {
       o.v[0] = pre;
 #pragma unroll
-      for (int e = 1; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e - 1] SCL_EXTRA_ARGS);
+      for (int e = 1; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e - 1] SCL_OP_ARGS);
     }
     if (reverse) {  // back to physical order
 #pragma unroll
@@ -574,13 +586,16 @@ scl_scan_s(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
         o.v[V - 1 - e] = t;
       }
     }
+    scl_pack<scl_O, V> m;
+#pragma unroll
+    for (int e = 0; e < V; ++e) m.v[e] = SCL_EPILOGUE(o.v[e]);
     if (ovec) {
-      scl_store<scl_T, V>(out + (tile_lo + pos), o);
+      scl_store<scl_O, V>(out + (tile_lo + pos), m);
     } else {
 #pragma unroll
       for (int e = 0; e < V; ++e) {
         const long long i = tile_lo + pos + e;
-        if (i >= c_lo && i < c_hi) out[i] = o.v[e];
+        if (i >= c_lo && i < c_hi) out[i] = m.v[e];
       }
     }
   }

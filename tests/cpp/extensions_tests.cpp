@@ -6,6 +6,7 @@
 
 #include <gtest/gtest.h>
 
+#include <SkelCL/Fused.h>
 #include <SkelCL/Graph.h>
 #include <SkelCL/Map.h>
 #include <SkelCL/Reduce.h>
@@ -91,6 +92,31 @@ TEST_F(ExtensionsTest, AutotunedMapGivesTheSameResult) {
     EXPECT_EQ(a[i], host[i] * 3 + 1);
     EXPECT_EQ(b[i], host[i] * 3 + 1);
   }
+}
+
+TEST_F(ExtensionsTest, FusedPairsEqualUnfused) {
+  const size_t n = (1 << 20) + 3;
+  std::vector<int> a(n), b(n);
+  for (size_t i = 0; i < n; ++i) {
+    a[i] = (int)(i % 97) - 48;
+    b[i] = (int)(i % 13) - 6;
+  }
+  skelcl::Vector<int> x(a.begin(), a.end()), y(b.begin(), b.end());
+  skelcl::Reduce<int(int)> sum("int func(int x, int y){ return x + y; }");
+  skelcl::Zip<int(int, int)> mul("int func(int x, int y){ return x * y; }");
+  skelcl::ZipReduce<int(int, int)> dot(sum, mul);
+  skelcl::Vector<int> d = dot(x, y);
+  long long want = 0;
+  for (size_t i = 0; i < n; ++i) want += (long long)a[i] * b[i];
+  EXPECT_EQ(d[0], (int)want);
+
+  skelcl::Scan<int(int)> scan("int func(int x, int y){ return x + y; }");
+  scan.setInclusive(true);
+  skelcl::Map<int(int)> mod("int func(int x){ return x % 7919; }");
+  skelcl::ScanMap<int(int)> fused(scan, mod);
+  skelcl::Vector<int> f = fused(x);
+  skelcl::Vector<int> u = mod(scan(x));
+  for (size_t i = 0; i < n; i += 101) EXPECT_EQ(f[i], u[i]);
 }
 
 int main(int argc, char** argv) {
