@@ -4,6 +4,9 @@
 #ifndef SKELCL_DEVICE_H_
 #define SKELCL_DEVICE_H_
 
+#include <cctype>
+#include <istream>
+#include <string>
 #include <cstddef>
 #include <memory>
 #include <string>
@@ -132,6 +135,21 @@ inline std::ostream& operator<<(std::ostream& os, Device::Type t) {
     case Device::DEFAULT: return os << "DEFAULT";
     default: return os << "ANY";
   }
+}
+
+// Reads ANY, ALL, CPU, GPU, ACCELERATOR or DEFAULT (command-line arguments of
+// type device_type); anything else sets the stream's fail bit.
+inline std::istream& operator>>(std::istream& is, Device::Type& t) {
+  std::string w;
+  is >> w;
+  for (char& c : w) c = (char)std::toupper((unsigned char)c);
+  if (w == "ANY" || w == "ALL") t = Device::ANY;
+  else if (w == "CPU") t = Device::CPU;
+  else if (w == "GPU") t = Device::GPU;
+  else if (w == "ACCELERATOR") t = Device::ACCELERATOR;
+  else if (w == "DEFAULT") t = Device::DEFAULT;
+  else is.setstate(std::ios::failbit);
+  return is;
 }
 
 }  // namespace detail
