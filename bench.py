@@ -217,6 +217,10 @@ def run_gpu(args):
     tkey = {"scan": "scan_int32_2^28", "map": "map_mod_int32_2^28"}[dominant]
 
     # ---- e2e through the C ABI with pinned host buffers -----------------------------
+    # Every step copies its input in (copy stream 1), runs Scan + Map (stream
+    # 0) and reads its result back (copy stream 2); two device buffer pairs
+    # let step k's input copy overlap step k-1's read-back (the host link
+    # carries ~0.2 TB/s each way, ~0.34 TB/s both ways at once).
     import ctypes
     L = S.lib()
     hin = ctypes.c_void_p()
@@ -224,17 +228,50 @@ def run_gpu(args):
     S.check(L.scl_host_alloc(4 * N_SCAN, ctypes.byref(hin)))
     S.check(L.scl_host_alloc(4 * N_SCAN, ctypes.byref(hout)))
     ctypes.memmove(hin, x.ctypes.data, 4 * N_SCAN)
+    dxs = [dx, S.DeviceArray(N_SCAN, np.int32)]
+    dys = [dy, S.DeviceArray(N_SCAN, np.int32)]
+    ev_in = [S.Event(), S.Event()]
+    ev_done = [S.Event(), S.Event()]
+    ev_out = [S.Event(), S.Event()]
 
-    def e2e_step():
-        S.check(L.scl_h2d_async(dx.ptr, hin, 4 * N_SCAN))
-        step()
-        S.check(L.scl_d2h_async(hout, dy.ptr, 4 * N_SCAN))
+    def e2e_step(k):
+        b = k % 2
+        if k >= 2:
+            ev_done[b].wait_on(1)  # step k-2 has read input buffer b
+        S.check(L.scl_h2d_on(1, dxs[b].ptr, hin, 4 * N_SCAN))
+        ev_in[b].record_on(1)
+        ev_in[b].wait_on(0)
+        if k >= 2:
+            ev_out[b].wait_on(0)   # step k-2's result has left output buffer b
+        scan.launch([dxs[b], dys[b]], n=N_SCAN, flags=S.SHAPE_INCLUSIVE)
+        mod.launch([dys[b], dys[b]], n=N_SCAN)
+        ev_done[b].record_on(0)
+        ev_done[b].wait_on(2)
+        S.check(L.scl_d2h_on(2, hout, dys[b].ptr, 4 * N_SCAN))
+        ev_out[b].record_on(2)
 
-    e2e_ms = timed(S, e2e_step, max(2, args.steps // 2), 1)
+    def e2e_run(steps):
+        e0, e1 = S.Event(), S.Event()
+        S.sync()
+        e0.record_on(0)
+        e0.wait_on(1)
+        for k in range(steps):
+            e2e_step(k)
+        ev_out[(steps - 1) % 2].wait_on(0)
+        e1.record_on(0)
+        S.sync()
+        return e0.elapsed_ms(e1) / steps
+
+    e2e_run(2)  # warm-up
+    e2e_steps = max(4, args.steps)
+    e2e_ms = e2e_run(e2e_steps)
+    hres = np.ctypeslib.as_array(ctypes.cast(hout, ctypes.POINTER(ctypes.c_int32)), shape=(N_SCAN,))
+    e2e_parity = bool(np.array_equal(hres, dy.to_numpy()))
     e2e_val = (BYTES_SCAN + BYTES_MAP) / (e2e_ms * 1e-3) / 1e9
+    del hres
     L.scl_host_free(hin)
     L.scl_host_free(hout)
-    del dx, dy
+    del dx, dy, dxs, dys
 
     line = {
         "metric": METRIC,
@@ -259,7 +296,10 @@ def run_gpu(args):
                      "traffic": traffic.get(tkey), "algorithmic_bytes": dom_bytes,
                      "per_kernel_ms": {"scan": round(scan_ms, 4), "map": round(map_ms, 4)}},
         "e2e": {"value": round(e2e_val, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * N_SCAN,
-                "d2h_bytes_per_step": 4 * N_SCAN, "ms_per_step": round(e2e_ms, 3)},
+                "d2h_bytes_per_step": 4 * N_SCAN, "ms_per_step": round(e2e_ms, 3), "steps": e2e_steps,
+                "result_matches_device": e2e_parity,
+                "note": "pinned host buffers; input copy, Scan+Map and result read-back of "
+                        "consecutive steps overlap on three streams"},
         "gpu_launches": launches,
         "clocks": clocks,
     }

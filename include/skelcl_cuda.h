@@ -192,11 +192,20 @@ int scl_memset(void* dst, int value, size_t bytes);
 int scl_host_alloc(size_t bytes, void** hptr); /* pinned host memory */
 int scl_host_free(void* hptr);
 int scl_sync(void);                 /* wait for the stream; reports device-side errors */
+/* Transfers on copy streams, to overlap them with launches (the reference
+ * enqueues transfers asynchronously on its command queues,
+ * src/Device.cpp:124-167, src/DeviceBuffer.cpp:60-135).  stream 0 is the
+ * library stream every launch runs on; 1 and 2 are copy streams.  Order
+ * streams with scl_event_record_on / scl_stream_wait; scl_sync waits for all. */
+int scl_h2d_on(int stream, void* dst, const void* src, size_t bytes);
+int scl_d2h_on(int stream, void* dst, const void* src, size_t bytes);
 
 /* ---- events: replaces detail::Event (src/Event.cpp) and the profiling queue */
 typedef struct scl_event scl_event;
 int scl_event_create(scl_event** ev);
 int scl_event_record(scl_event* ev);
+int scl_event_record_on(scl_event* ev, int stream);  /* see scl_h2d_on            */
+int scl_stream_wait(int stream, scl_event* ev);       /* `stream` waits for `ev`   */
 int scl_event_elapsed_ms(scl_event* start, scl_event* stop, float* ms);
 int scl_event_destroy(scl_event* ev);
 

@@ -107,6 +107,8 @@ SIGNATURES = {
     "scl_adjoint_accumulate": ([_VP, _VP, _U64, _I], _I),
     "scl_adjoint_broadcast_segments": ([_VP, _VP, _VP, _U64, _U64, _I, _I], _I),
     "scl_autotune_set": ([_I], _I), "scl_autotune_get": ([ctypes.POINTER(_I)], _I),
+    "scl_h2d_on": ([_I, _VP, _VP, _SZ], _I), "scl_d2h_on": ([_I, _VP, _VP, _SZ], _I),
+    "scl_event_record_on": ([_VP, _I], _I), "scl_stream_wait": ([_I, _VP], _I),
     "scl_mapoverlap_adjoint_edges": ([_VP, _VP, _VP, _U64, _U64, _I], _I),
 }
 
@@ -363,6 +365,14 @@ class Event:
 
     def record(self) -> None:
         check(lib().scl_event_record(self.handle))
+
+    def record_on(self, stream: int) -> None:
+        """Record on stream 0 (launches) or copy stream 1 / 2."""
+        check(lib().scl_event_record_on(self.handle, stream))
+
+    def wait_on(self, stream: int) -> None:
+        """Make `stream` wait for this event."""
+        check(lib().scl_stream_wait(stream, self.handle))
 
     def elapsed_ms(self, later: "Event") -> float:
         ms = ctypes.c_float(0)

@@ -67,6 +67,7 @@ struct Runtime {
   size_t global_mem = 0;
   std::string name;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_streams[2] = {nullptr, nullptr};  // transfers that overlap launches
   unsigned int* dev_err = nullptr;   // device-side status word
   unsigned int* host_err = nullptr;  // pinned mirror
   uint64_t launches = 0;

@@ -124,6 +124,7 @@ extern "C" int scl_init(int device) {
   g_rt.global_mem = prop.totalGlobalMem;
   g_rt.name = prop.name;
   SCL_CUDA(cudaStreamCreateWithFlags(&g_rt.stream, cudaStreamNonBlocking));
+  for (cudaStream_t& c : g_rt.copy_streams) SCL_CUDA(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
     uint64_t thresh = UINT64_MAX;
@@ -143,6 +144,11 @@ extern "C" int scl_terminate(void) {
   cudaStreamSynchronize(g_rt.stream);
   cudaFree(g_rt.dev_err);
   cudaFreeHost(g_rt.host_err);
+  for (cudaStream_t& c : g_rt.copy_streams) {
+    cudaStreamSynchronize(c);
+    cudaStreamDestroy(c);
+    c = nullptr;
+  }
   cudaStreamDestroy(g_rt.stream);
   g_rt.dev_err = nullptr;
   g_rt.host_err = nullptr;
@@ -246,8 +252,35 @@ extern "C" int scl_host_free(void* hptr) {
 }
 extern "C" int scl_sync(void) {
   if (int st = require_init()) return st;
+  for (cudaStream_t c : g_rt.copy_streams) SCL_CUDA(cudaStreamSynchronize(c));
   SCL_CUDA(cudaStreamSynchronize(g_rt.stream));
   return check_device_status();
+}
+
+// ---- copy streams ----------------------------------------------------------------
+namespace {
+int stream_of(int s, cudaStream_t* out) {
+  if (s == 0) *out = g_rt.stream;
+  else if (s == 1 || s == 2) *out = g_rt.copy_streams[s - 1];
+  else return fail(SCL_ERR_ARG, "stream must be 0 (launches), 1 or 2 (copies)");
+  return SCL_OK;
+}
+int copy_on(int s, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+  if (int st = require_init()) return st;
+  if (bytes == 0) return SCL_OK;
+  if (!dst || !src) return fail(SCL_ERR_ARG, "copy: null pointer");
+  cudaStream_t cs;
+  if (int st = stream_of(s, &cs)) return st;
+  SCL_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, cs));
+  return SCL_OK;
+}
+}  // namespace
+
+extern "C" int scl_h2d_on(int stream, void* dst, const void* src, size_t bytes) {
+  return copy_on(stream, dst, src, bytes, cudaMemcpyHostToDevice);
+}
+extern "C" int scl_d2h_on(int stream, void* dst, const void* src, size_t bytes) {
+  return copy_on(stream, dst, src, bytes, cudaMemcpyDeviceToHost);
 }
 
 // ---- events -------------------------------------------------------------------
@@ -270,6 +303,22 @@ extern "C" int scl_event_record(scl_event* ev) {
   if (int st = require_init()) return st;
   if (!ev) return fail(SCL_ERR_ARG, "null event");
   SCL_CUDA(cudaEventRecord(ev->ev, g_rt.stream));
+  return SCL_OK;
+}
+extern "C" int scl_event_record_on(scl_event* ev, int stream) {
+  if (int st = require_init()) return st;
+  if (!ev) return fail(SCL_ERR_ARG, "null event");
+  cudaStream_t cs;
+  if (int st = stream_of(stream, &cs)) return st;
+  SCL_CUDA(cudaEventRecord(ev->ev, cs));
+  return SCL_OK;
+}
+extern "C" int scl_stream_wait(int stream, scl_event* ev) {
+  if (int st = require_init()) return st;
+  if (!ev) return fail(SCL_ERR_ARG, "null event");
+  cudaStream_t cs;
+  if (int st = stream_of(stream, &cs)) return st;
+  SCL_CUDA(cudaStreamWaitEvent(cs, ev->ev, 0));
   return SCL_OK;
 }
 extern "C" int scl_event_elapsed_ms(scl_event* a, scl_event* b, float* ms) {
