@@ -119,6 +119,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(value: float, dist) -> float:
+    """The slowest rank's time (replicas run the same work: the job takes as
+    long as its slowest GPU).  `dist` is torch.distributed or None."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def timed(S, fn, steps: int, warmup: int, kernel_events=None):
     """Warm-up, then time exactly `steps` calls of fn with events on the
     library stream (synchronised on both sides)."""
@@ -199,12 +210,7 @@ def run_gpu(args):
         per_kernel["map"].append(e[1].elapsed_ms(e[2]))
     launches = S.launch_count() - launches0
     clocks = sampler.stop()
-    ms_step = ms_total / args.steps
-    if dist:
-        import torch
-        t = torch.tensor([ms_step], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = max_over_ranks(ms_total / args.steps, dist)
     value = world * (BYTES_SCAN + BYTES_MAP) / (ms_step * 1e-3) / 1e9
 
     scan_ms = statistics.mean(per_kernel["scan"])
