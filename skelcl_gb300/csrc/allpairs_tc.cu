@@ -140,7 +140,10 @@ __global__ void split_transpose_kernel(const float* __restrict__ B, uint32_t K, 
   }
 }
 
-template <int PARTS, int STAGES>
+// G = k-blocks accumulated in tensor memory between two drains into the
+// epilogue's FP32 registers (1: every 64-wide k-block; larger G drains less
+// often at a longer in-TMEM accumulation chain).
+template <int PARTS, int STAGES, int G>
 __global__ void __launch_bounds__(THREADS, 1)
 gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    float* __restrict__ P, uint32_t M, uint32_t N, uint32_t Kp, uint32_t spin_limit,
@@ -233,9 +236,13 @@ gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
       }
       for (uint32_t kb = 0; kb < nk; ++kb) {
         const int s = (int)(kb % STAGES);
-        const int acc_i = (int)(kb & 1u);
-        const uint32_t use = kb >> 1;  // how often this accumulator was used before
-        if (use > 0 && !mbar_wait(smem_u32(&acc_empty[acc_i]), (use - 1) & 1u, spin_limit)) {
+        const uint32_t grp = kb / G;          // drain group of this k-block
+        const bool first_in_grp = kb % G == 0;
+        const bool last_in_grp = kb % G == G - 1 || kb + 1 == nk;
+        const int acc_i = (int)(grp & 1u);
+        const uint32_t use = grp >> 1;  // how often this accumulator was used before
+        if (first_in_grp && use > 0 &&
+            !mbar_wait(smem_u32(&acc_empty[acc_i]), (use - 1) & 1u, spin_limit)) {
           raise(err);
           s_fail = 1;
           break;
@@ -257,7 +264,7 @@ gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
             // advance 16 bf16 = 32 bytes along K inside the swizzle row
             const uint64_t a = ad + (uint64_t)(ks * 2);
             const uint64_t b = bd + (uint64_t)(ks * 2);
-            const uint32_t acc = (q > 0 || ks > 0) ? 1u : 0u;  // fresh partial per k-block
+            const uint32_t acc = (!first_in_grp || q > 0 || ks > 0) ? 1u : 0u;  // fresh per group
             asm volatile(
                 "{ .reg .pred p; setp.ne.b32 p, %4, 0;"
                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }"
@@ -268,9 +275,10 @@ gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
             :: "r"(smem_u32(&empty_bar[s])) : "memory");
-        asm volatile(
-            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-            :: "r"(smem_u32(&acc_full[acc_i])) : "memory");
+        if (last_in_grp)
+          asm volatile(
+              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+              :: "r"(smem_u32(&acc_full[acc_i])) : "memory");
       }
       // no MMA may still run when the tensor memory is freed (also after a
       // failed wait above)
@@ -287,9 +295,10 @@ gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
 #pragma unroll
     for (int j = 0; j < BN; ++j) sum[j] = 0.0f;
     bool ok = true;
-    for (uint32_t kb = 0; kb < nk; ++kb) {
-      const int acc_i = (int)(kb & 1u);
-      if (!mbar_wait(smem_u32(&acc_full[acc_i]), (kb >> 1) & 1u, spin_limit)) {
+    const uint32_t ngrp = (nk + G - 1) / G;
+    for (uint32_t grp = 0; grp < ngrp; ++grp) {
+      const int acc_i = (int)(grp & 1u);
+      if (!mbar_wait(smem_u32(&acc_full[acc_i]), (grp >> 1) & 1u, spin_limit)) {
         if (lane == 0) raise(err);
         ok = false;
         break;
@@ -395,8 +404,22 @@ static int encode_parts(CUtensorMap* tm, void* base, uint64_t rows, uint64_t Kp,
   return SCL_OK;
 }
 
+namespace {
+template <int PARTS, int STAGES, int G>
+cudaError_t launch_gemm(dim3 grid, cudaStream_t stream, const CUtensorMap& tmA, const CUtensorMap& tmB,
+                        float* P, uint32_t M, uint32_t N, uint32_t Kp, uint32_t spin_limit,
+                        unsigned int* err) {
+  const size_t smem = (size_t)STAGES * 2 * PARTS * tc::TILE_BYTES + 1024;
+  auto kern = tc::gemm_3xbf16_kernel<PARTS, STAGES, G>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, tc::THREADS, smem, stream>>>(tmA, tmB, P, M, N, Kp, spin_limit, err);
+  return cudaGetLastError();
+}
+}  // namespace
+
 int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uint32_t N,
-                       uint32_t K, int parts, int trans, void* scratch, size_t scratch_bytes,
+                       uint32_t K, int parts, int trans, int drain, void* scratch, size_t scratch_bytes,
                        cudaStream_t stream, uint32_t spin_limit, unsigned int* err) {
   if (parts != 2 && parts != 3) return fail(SCL_ERR_ARG, "3xBF16: parts must be 2 or 3");
   const uint32_t Mp = tc::round_up(M, tc::BM), Np = tc::round_up(N, tc::BN),
@@ -431,23 +454,17 @@ int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uin
 
   dim3 grid(Np / tc::BN, Mp / tc::BM);
   if (grid.y > 65535) return fail(SCL_ERR_ARG, "3xBF16: too many row tiles");
+  // parts 3: 2 stages of 96 KB; parts 2: 3 stages of 64 KB
   cudaError_t e;
   if (parts == 3) {
-    constexpr int STAGES = 2;
-    const size_t smem = (size_t)STAGES * 2 * 3 * tc::TILE_BYTES + 1024;
-    auto kern = tc::gemm_3xbf16_kernel<3, STAGES>;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(3xbf16)");
-    kern<<<grid, tc::THREADS, smem, stream>>>(tmA, tmB, P, M, N, Kp, spin_limit, err);
+    e = drain >= 4 ? launch_gemm<3, 2, 4>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
+      : drain == 2 ? launch_gemm<3, 2, 2>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
+                   : launch_gemm<3, 2, 1>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err);
   } else {
-    constexpr int STAGES = 3;
-    const size_t smem = (size_t)STAGES * 2 * 2 * tc::TILE_BYTES + 1024;
-    auto kern = tc::gemm_3xbf16_kernel<2, STAGES>;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(3xbf16)");
-    kern<<<grid, tc::THREADS, smem, stream>>>(tmA, tmB, P, M, N, Kp, spin_limit, err);
+    e = drain >= 4 ? launch_gemm<2, 3, 4>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
+      : drain == 2 ? launch_gemm<2, 3, 2>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
+                   : launch_gemm<2, 3, 1>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err);
   }
-  e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "3xBF16 launch");
   rt().launches += 1;
   return SCL_OK;

@@ -12,7 +12,7 @@
 // tcgen05 contraction (allpairs_tc.cu)
 namespace scl {
 int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uint32_t N,
-                       uint32_t K, int parts, int trans, void* scratch, size_t scratch_bytes,
+                       uint32_t K, int parts, int trans, int drain, void* scratch, size_t scratch_bytes,
                        cudaStream_t stream, uint32_t spin_limit, unsigned int* err);
 // row-major rows x cols -> cols x rows, elements of 4 or 8 bytes (adjoint.cu)
 int transpose_launch(const void* src, void* dst, uint64_t rows, uint64_t cols, size_t elem,
@@ -621,8 +621,10 @@ extern "C" int scl_launch_allpairs(scl_program* p, const scl_shape* sh, void* co
       const size_t need = allpairs_tc_scratch_bytes(M, N, K, parts);
       if (int st = ensure_workspace(p, need)) return st;
       p->last_variant = SCL_VARIANT_TC3XBF16;
+      // tuning.tile_w: k-blocks accumulated in tensor memory per drain (1, 2 or 4)
+      const int drain = (tu && tu->tile_w) ? (int)tu->tile_w : 1;
       return allpairs_tc_launch((const float*)A, (const float*)B, (float*)P, M, N, K, parts, trans,
-                                p->ws.ptr, p->ws.bytes, rt().stream, spin_of(tu), rt().dev_err);
+                                drain, p->ws.ptr, p->ws.bytes, rt().stream, spin_of(tu), rt().dev_err);
     }
     if (want == SCL_VARIANT_TC3XBF16)
       return fail(SCL_ERR_UNSUPPORTED, "the tensor-core AllPairs needs zip x*y, reduce x+y, identity 0, "
