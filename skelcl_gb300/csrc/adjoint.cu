@@ -76,12 +76,15 @@ __global__ void accumulate_kernel(T* __restrict__ dst, const T* __restrict__ src
 // in[clamp(y+dy)][clamp(x+dx)]; every read position p' outside the matrix
 // was served by the edge pixel clamp(p').  Its adjoint therefore adds, to each
 // edge pixel p, the zero-padded transposed stencil of g evaluated at every
-// outside position p' with clamp(p') = p.  One thread per edge pixel.
+// outside position p' with clamp(p') = p.  One warp per edge pixel: the lanes
+// share the taps, loop over the outside positions, and add their sums with
+// shuffles.
 __global__ void stencil_edges_kernel(const float* __restrict__ g, const float* __restrict__ w,
                                      float* __restrict__ gin, int64_t rows, int64_t cols, int R,
                                      int64_t n_edge) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n_edge) return;
+  const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (e >= n_edge) return;  // whole warps leave together (blockDim is a multiple of 32)
   int64_t y, x;
   // top row, bottom row (rows > 1), left column, right column (cols > 1),
   // the columns without their first and last pixels
@@ -100,22 +103,24 @@ __global__ void stencil_edges_kernel(const float* __restrict__ g, const float* _
   const int64_t x0 = (x == 0) ? -R : x, x1 = (x == cols - 1) ? cols - 1 + R : x;
   const int W = 2 * R + 1;
   float acc = 0.0f;
-  for (int64_t py = y0; py <= y1; ++py)
-    for (int64_t px = x0; px <= x1; ++px) {
-      if (py == y && px == x) continue;  // inside: already in gin
-      float s = 0.0f;
-      for (int dy = -R; dy <= R; ++dy) {
-        const int64_t qy = py + dy;
-        if (qy < 0 || qy >= rows) continue;
-        for (int dx = -R; dx <= R; ++dx) {
-          const int64_t qx = px + dx;
-          if (qx < 0 || qx >= cols) continue;
-          s += w[(dy + R) * W + (dx + R)] * g[qy * cols + qx];
-        }
+  // each lane takes every 32nd tap, and for it every outside position
+  for (int tap = lane; tap < W * W; tap += 32) {
+    const int dy = tap / W - R, dx = tap % W - R;
+    const float wt = w[tap];
+    for (int64_t py = y0; py <= y1; ++py) {
+      const int64_t qy = py + dy;
+      if (qy < 0 || qy >= rows) continue;
+      for (int64_t px = x0; px <= x1; ++px) {
+        if (py == y && px == x) continue;  // inside: already in gin
+        const int64_t qx = px + dx;
+        if (qx < 0 || qx >= cols) continue;
+        acc += wt * g[qy * cols + qx];
       }
-      acc += s;
     }
-  gin[y * cols + x] += acc;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) gin[y * cols + x] += acc;
 }
 
 template <typename T>
@@ -203,9 +208,9 @@ extern "C" int scl_mapoverlap_adjoint_edges(const float* g, const float* w, floa
   if (R == 0) return SCL_OK;
   const int64_t r = (int64_t)rows, c = (int64_t)cols;
   const int64_t n_edge = c + (r > 1 ? c : 0) + (r > 2 ? r - 2 : 0) * (c > 1 ? 2 : 1);
-  const int64_t grid = (n_edge + 127) / 128;
+  const int64_t grid = (n_edge + 7) / 8;  // 8 warps (edge pixels) per block
   if (grid > 0x7fffffffll) return fail(SCL_ERR_ARG, "stencil adjoint: matrix too large");
-  stencil_edges_kernel<<<(unsigned)grid, 128, 0, rt().stream>>>(g, w, gin, r, c, R, n_edge);
+  stencil_edges_kernel<<<(unsigned)grid, 256, 0, rt().stream>>>(g, w, gin, r, c, R, n_edge);
   SCL_CUDA(cudaGetLastError());
   ++rt().launches;
   return SCL_OK;

@@ -15,6 +15,14 @@ def dev(a):
     return S.DeviceArray.from_numpy(np.ascontiguousarray(a))
 
 
+def test_zip_reduce_empty_gives_identity(scl):
+    p = S.Program(S.KIND_ZIP_REDUCE, "int func(int x, int y){ return x + y; }", ["int"] * 3,
+                  source2="int m(int x, int y){ return x * y; }", func2="m", identity="0")
+    out = dev(np.array([12345], np.int32))
+    p.launch([out, out, out], n=0)
+    assert out.to_numpy()[0] == 0
+
+
 @pytest.mark.parametrize("n", [1, 5, 4099, 1 << 24])
 def test_zip_reduce_dot_product(scl, orc, n):
     x = orc.uniform_f32(n, 0, -1.0, 1.0)
