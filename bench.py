@@ -430,8 +430,18 @@ def secondary(S, oracle, hbm_peak, args):
         "adjoint_GBps": round(8 * n / bwd / 1e6, 1),
         "fwd_plus_adjoint_over_fwd": round((fwd + bwd) / fwd, 3),
         "max_abs_err_vs_fp64": float(np.abs(yf - ref).max()),
-        "max_abs_prefix": float(np.abs(ref).max())}
+        "max_abs_prefix": float(np.abs(ref).max()),
+        "note": "about 15 us per call is fixed (status clear, launch, ramp): 2^28 below"}
     del dxf, dg, dyf, dgx, yf, ref
+    n4 = 1 << 28
+    dxf, dyf = S.DeviceArray.from_numpy(oracle.uniform_f32(n4, 2, -1.0, 1.0)), S.DeviceArray(n4, np.float32)
+    fwd4 = timed(S, lambda: sp.launch([dxf, dyf], n=n4, flags=S.SHAPE_INCLUSIVE), 10, 3)
+    bwd4 = timed(S, lambda: sp.launch([dxf, dyf], n=n4, flags=S.SHAPE_INCLUSIVE | S.SHAPE_REVERSE), 10, 3)
+    out["float_scan_2^28"] = {"fwd_GBps": round(8 * n4 / fwd4 / 1e6, 1),
+                              "fwd_frac": round(8 * n4 / fwd4 / 1e6 / hbm_peak, 3),
+                              "adjoint_GBps": round(8 * n4 / bwd4 / 1e6, 1),
+                              "fwd_plus_adjoint_over_fwd": round((fwd4 + bwd4) / fwd4, 3)}
+    del dxf, dyf
 
     # MapOverlap 8192^2, R = 5 Gaussian, both paddings
     rows = cols = 8192
