@@ -7,7 +7,7 @@
 // K x N row-major (AllPairsKernel.cl:72).  Extra arguments: the Reduce's
 // first, then the Zip's (AllPairsDef.h:265-269).
 // Shape: 128 x 128 output tile per 256-thread block, 8 x 8 register
-// accumulators per thread, k-tiles of 8 double-buffered in shared memory
+// accumulators per thread, k-tiles of 16 double-buffered in shared memory
 // with the next tile prefetched into registers.  Unlike the reference, P is
 // written once (the reference re-reads and re-writes P every 32-wide k
 // segment, AllPairsKernel.cl:77-78,95-96).
@@ -20,12 +20,17 @@
 #if SCL_KIND == 12
 #define SCL_AP_BM 128
 #define SCL_AP_BN 128
-#define SCL_AP_BK 8
+// k-tile: 16 for 4-byte operands, 8 for wider ones (48 KB of static shared memory)
+#define SCL_AP_BK ((sizeof(SCL_TYPE_0) <= 4 && sizeof(SCL_TYPE_1) <= 4) ? 16 : 8)
 typedef SCL_TYPE_0 scl_L;
 typedef SCL_TYPE_1 scl_Rt;
 typedef SCL_TYPE_2 scl_O;
 
-extern "C" __global__ void __launch_bounds__(256)
+// Thread (tx, ty) of the 16 x 16 block owns rows {ty*4 .. +3, 64 + ty*4 .. +3}
+// and columns {tx*4 .. +3, 64 + tx*4 .. +3} of the 128 x 128 tile: its
+// shared-memory reads are 16-byte loads that a warp spreads over all banks.
+// two blocks per SM when the accumulators are 4-byte values
+extern "C" __global__ void __launch_bounds__(256, sizeof(SCL_TYPE_2) <= 4 ? 2 : 1)
 scl_allpairs_simt(const scl_L* A, const scl_Rt* B, scl_O* P, unsigned int M, unsigned int N,
                   unsigned int K, int vec_a, int vec_b SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
@@ -34,39 +39,68 @@ scl_allpairs_simt(const scl_L* A, const scl_Rt* B, scl_O* P, unsigned int M, uns
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const unsigned int m0 = blockIdx.y * SCL_AP_BM, n0 = blockIdx.x * SCL_AP_BN;
-  // global -> register mapping: A tile 128 rows x 8 k (row = tid/2, k = (tid&1)*4 ..+4),
-  // B tile 8 k x 128 cols (k = tid/32, col = (tid&31)*4 ..+4)
-  const int a_row = tid >> 1, a_k = (tid & 1) * 4;
-  const int b_k = tid >> 5, b_col = (tid & 31) * 4;
-  scl_L ra[4];
-  scl_Rt rb[4];
+  // global -> register mapping: A tile 128 rows x BK k (row = tid/2, AE
+  // consecutive k per thread), B tile BK k x 128 cols (BE consecutive columns)
+  constexpr int BK = SCL_AP_BK, AE = BK / 2, TPR = 256 / BK, BE = SCL_AP_BN / TPR;
+  const int a_row = tid >> 1, a_k = (tid & 1) * AE;
+  const int b_k = tid / TPR, b_col = (tid % TPR) * BE;
+  scl_L ra[AE];
+  scl_Rt rb[BE];
   auto load_tile = [&](unsigned int k0) {
-    const unsigned int gm = m0 + a_row, gk = k0 + a_k;
-    if (vec_a && gm < M && gk + 3 < K) {
-      scl_pack<scl_L, 4> p = scl_load<scl_L, 4>(A + (scl_u64)gm * K + gk);
+    const unsigned int gm = m0 + a_row;
 #pragma unroll
-      for (int i = 0; i < 4; ++i) ra[i] = p.v[i];
-    } else {
+    for (int h = 0; h < AE / 4; ++h) {
+      const unsigned int gk = k0 + a_k + h * 4;
+      if (vec_a && gm < M && gk + 3 < K) {
+        scl_pack<scl_L, 4> p = scl_load<scl_L, 4>(A + (scl_u64)gm * K + gk);
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
-        ra[i] = (gm < M && gk + i < K) ? A[(scl_u64)gm * K + gk + i] : (scl_L)0;
+        for (int i = 0; i < 4; ++i) ra[h * 4 + i] = p.v[i];
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          ra[h * 4 + i] = (gm < M && gk + i < K) ? A[(scl_u64)gm * K + gk + i] : (scl_L)0;
+      }
     }
-    const unsigned int bk = k0 + b_k, bn = n0 + b_col;
-    if (vec_b && bk < K && bn + 3 < N) {
-      scl_pack<scl_Rt, 4> p = scl_load<scl_Rt, 4>(B + (scl_u64)bk * N + bn);
+    const unsigned int bk = k0 + b_k;
 #pragma unroll
-      for (int i = 0; i < 4; ++i) rb[i] = p.v[i];
-    } else {
+    for (int h = 0; h < BE / 4; ++h) {
+      const unsigned int bn = n0 + b_col + h * 4;
+      if (vec_b && bk < K && bn + 3 < N) {
+        scl_pack<scl_Rt, 4> p = scl_load<scl_Rt, 4>(B + (scl_u64)bk * N + bn);
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
-        rb[i] = (bk < K && bn + i < N) ? B[(scl_u64)bk * N + bn + i] : (scl_Rt)0;
+        for (int i = 0; i < 4; ++i) rb[h * 4 + i] = p.v[i];
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          rb[h * 4 + i] = (bk < K && bn + i < N) ? B[(scl_u64)bk * N + bn + i] : (scl_Rt)0;
+      }
     }
   };
   auto store_tile = [&](int buf) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) As[buf][a_k + i][a_row] = ra[i];
+    for (int i = 0; i < AE; ++i) As[buf][a_k + i][a_row] = ra[i];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) Bs[buf][b_k][b_col + i] = rb[i];
+    for (int i = 0; i < BE; ++i) Bs[buf][b_k][b_col + i] = rb[i];
+  };
+  auto step = [&](scl_O (&acc)[8][8], int cur, int kk) {
+    scl_L a[8];
+    scl_Rt b[8];
+    const scl_pack<scl_L, 4> a0 = scl_load<scl_L, 4>(&As[cur][kk][ty * 4]);
+    const scl_pack<scl_L, 4> a1 = scl_load<scl_L, 4>(&As[cur][kk][64 + ty * 4]);
+    const scl_pack<scl_Rt, 4> b0 = scl_load<scl_Rt, 4>(&Bs[cur][kk][tx * 4]);
+    const scl_pack<scl_Rt, 4> b1 = scl_load<scl_Rt, 4>(&Bs[cur][kk][64 + tx * 4]);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      a[i] = a0.v[i];
+      a[4 + i] = a1.v[i];
+      b[i] = b0.v[i];
+      b[4 + i] = b1.v[i];
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        acc[i][j] = USR_REDUCE(acc[i][j], USR_ZIP(a[i], b[j] SCL_ZIP_ARGS) SCL_REDUCE_ARGS);
   };
 
   scl_O acc[8][8];
@@ -85,45 +119,32 @@ scl_allpairs_simt(const scl_L* A, const scl_Rt* B, scl_O* P, unsigned int M, uns
     const unsigned int kmax = min((unsigned int)SCL_AP_BK, K - kt * SCL_AP_BK);
     if (kmax == SCL_AP_BK) {
 #pragma unroll
-      for (int kk = 0; kk < SCL_AP_BK; ++kk) {
-        scl_L a[8];
-        scl_Rt b[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) a[i] = As[cur][kk][ty * 8 + i];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) b[j] = Bs[cur][kk][tx * 8 + j];
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-          for (int j = 0; j < 8; ++j)
-            acc[i][j] = USR_REDUCE(acc[i][j], USR_ZIP(a[i], b[j] SCL_ZIP_ARGS) SCL_REDUCE_ARGS);
-      }
+      for (int kk = 0; kk < SCL_AP_BK; ++kk) step(acc, cur, kk);
     } else {
-      for (unsigned int kk = 0; kk < kmax; ++kk) {
-        scl_L a[8];
-        scl_Rt b[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) a[i] = As[cur][kk][ty * 8 + i];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) b[j] = Bs[cur][kk][tx * 8 + j];
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-          for (int j = 0; j < 8; ++j)
-            acc[i][j] = USR_REDUCE(acc[i][j], USR_ZIP(a[i], b[j] SCL_ZIP_ARGS) SCL_REDUCE_ARGS);
-      }
+      for (unsigned int kk = 0; kk < kmax; ++kk) step(acc, cur, (int)kk);
     }
     if (kt + 1 < ktiles) store_tile(cur ^ 1);
     __syncthreads();
   }
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    const unsigned int gm = m0 + ty * 8 + i;
+    const unsigned int gm = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
     if (gm >= M) continue;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const unsigned int gn = n0 + tx * 8 + j;
-      if (gn < N) P[(scl_u64)gm * N + gn] = acc[i][j];
+    for (int h = 0; h < 2; ++h) {
+      const unsigned int gn = n0 + h * 64 + tx * 4;
+      scl_O* dst = P + (scl_u64)gm * N + gn;
+      if (sizeof(scl_O) == 4 && (N % 4u) == 0 && gn + 3 < N &&
+          (((scl_u64)dst) & 15u) == 0) {
+        scl_pack<scl_O, 4> o;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) o.v[j] = acc[i][h * 4 + j];
+        scl_store<scl_O, 4>(dst, o);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (gn + j < N) dst[j] = acc[i][h * 4 + j];
+      }
     }
   }
 }
