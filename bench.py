@@ -473,7 +473,11 @@ def secondary(S, oracle, hbm_peak, args):
                 S.check(L.scl_mapoverlap_adjoint_edges(dg.ptr, dwt.ptr, do.ptr, rows, cols, 5))
 
         a_ms = timed(S, adjoint, 10, 3)
-        mo[name] = {"GBps": round(gbps, 1), "hbm_frac": round(gbps / hbm_peak, 3),
+        p.launch([di, do], rows=rows, cols=cols, extra=S.buffer(dw))
+        ref = oracle.stencil_f64(img.reshape(rows, cols), 5, w, pad, 0.0)
+        err = float(np.abs(do.to_numpy().reshape(rows, cols) - ref).max())
+        del ref
+        mo[name] = {"max_abs_err_vs_fp64": err, "GBps": round(gbps, 1), "hbm_frac": round(gbps / hbm_peak, 3),
                     "TFLOPs": round(tflops, 2), "fp32_frac_nominal": round(tflops / fp32_peak, 3),
                     "variant": p.last_variant, "adjoint_ms": round(a_ms, 4), "fwd_ms": round(ms, 4),
                     "fwd_plus_adjoint_over_fwd": round((ms + a_ms) / ms, 3)}
