@@ -494,9 +494,13 @@ def secondary(S, oracle, hbm_peak, args):
     res = {}
     rows_chk = np.arange(0, M, M // 16)
     ref = oracle.gemm_f64(A.reshape(M, K)[rows_chk], B.reshape(K, N))
-    for name, var, items in (("fp32_simt", S.VARIANT_SIMT, 0), ("tc_3xbf16_6prod", S.VARIANT_TC3XBF16, 3),
-                             ("tc_3xbf16_3prod", S.VARIANT_TC3XBF16, 2)):
-        tun = S.Tuning(variant=var, items=items)
+    # the tensor-core launches take 128 x 256 output tiles here (automatic
+    # choice); "_128col" repeats the 6-product one with 128 x 128 tiles
+    for name, var, items, cols in (("fp32_simt", S.VARIANT_SIMT, 0, 0),
+                                   ("tc_3xbf16_6prod", S.VARIANT_TC3XBF16, 3, 0),
+                                   ("tc_3xbf16_6prod_128col", S.VARIANT_TC3XBF16, 3, 128),
+                                   ("tc_3xbf16_3prod", S.VARIANT_TC3XBF16, 2, 0)):
+        tun = S.Tuning(variant=var, items=items, tile_h=cols)
         ms = timed(S, lambda: ap.launch([dA, dB, dP], rows=M, cols=N, dim=K, tuning=tun), 3, 1)
         P = dP.to_numpy().reshape(M, N)
         err = np.abs(P[rows_chk].astype(np.float64) - ref)

@@ -140,7 +140,7 @@ typedef struct scl_tuning {
   uint32_t workgroup;    /* threads per block                                 */
   uint32_t items;        /* vector rows per thread (Map/Zip/Reduce/Scan)       */
   uint32_t tile_w;       /* MapOverlap tile width / AllPairs tile             */
-  uint32_t tile_h;       /* MapOverlap rows per thread                        */
+  uint32_t tile_h;       /* MapOverlap rows per thread / AllPairs tile columns */
   uint32_t variant;      /* SCL_VARIANT_*                                     */
   uint32_t spin_limit;   /* bounded-wait polls before SCL_ERR_TIMEOUT, 0 = default */
 } scl_tuning;

@@ -40,30 +40,45 @@ namespace scl {
 namespace tc {
 
 constexpr int BM = 128;
-constexpr int BN = 128;
-constexpr int BK = 64;                           // one 128-byte swizzle row of bf16
-constexpr int TILE_BYTES = BM * BK * 2;          // 16 KB per operand part and stage
-constexpr uint32_t TMEM_COLS = 2 * BN;           // two FP32 accumulators (ping-pong)
-constexpr int THREADS = 192;                     // 6 warps
+constexpr int NPAD = 256;                        // N padding: fits both tile widths
+constexpr int KPAD = 64;                         // K padding: whole k-blocks of both shapes
 
-// Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
-// (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits
-// 17-22, M >> 4 in bits 24-28.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+// Tile shape by output-tile width BN_T: 128 x 128 tiles take k-blocks of 64
+// (one 128-byte SWIZZLE_128B row of bf16) with 4 epilogue warps; 128 x 256
+// tiles take k-blocks of 32 (one 64-byte SWIZZLE_64B row, so that three
+// stages of six parts fit in shared memory) with 8 epilogue warps, and read
+// each A tile for twice as many columns.
+template <int BN_T>
+struct Shape {
+  static constexpr int BN = BN_T;
+  static constexpr int BK = BN_T == 256 ? 32 : 64;
+  static constexpr int A_TILE = BM * BK * 2;     // bytes of one A part per stage
+  static constexpr int B_TILE = BN * BK * 2;     // bytes of one B part per stage
+  static constexpr int EPI_WARPS = BN / 32;      // each drains 32 rows x 128 columns
+  static constexpr int THREADS = 64 + 32 * EPI_WARPS;
+  static constexpr uint32_t TMEM_COLS = 2 * BN;  // two FP32 accumulators (ping-pong)
+  static constexpr uint32_t SBO = 8 * BK * 2;    // bytes between 8-row groups
+  static constexpr uint64_t LAYOUT = BK == 64 ? 2u : 4u;  // SWIZZLE_128B : SWIZZLE_64B
+  // Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
+  // (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits
+  // 17-22, M >> 4 in bits 24-28.
+  static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) |
+                                    ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+};
 
-// Shared-memory matrix descriptor for a K-major SWIZZLE_128B tile whose rows
-// are 128 bytes and whose 8-row groups are 1024 bytes apart: start address
-// >> 4 (bits 0-13), leading-byte offset 1 (unused for swizzled K-major),
-// stride-byte offset 1024 >> 4 (bits 32-45), descriptor version 1 (bits
-// 46-47), layout SWIZZLE_128B = 2 (bits 61-63).
+// Shared-memory matrix descriptor for a K-major swizzled tile (rows of BK
+// bf16, 8-row groups SBO bytes apart): start address >> 4 (bits 0-13),
+// leading-byte offset 1 (unused for swizzled K-major), stride-byte offset >> 4
+// (bits 32-45), descriptor version 1 (bits 46-47), layout (bits 61-63).
+template <int BN_T>
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+  using SH = Shape<BN_T>;
   uint64_t d = 0;
   d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
   d |= (uint64_t)1u << 16;
-  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)(SH::SBO >> 4) << 32;
   d |= (uint64_t)1u << 46;
-  d |= (uint64_t)2u << 61;
+  d |= SH::LAYOUT << 61;
   return d;
 }
 
@@ -141,14 +156,18 @@ __global__ void split_transpose_kernel(const float* __restrict__ B, uint32_t K, 
 }
 
 // G = k-blocks accumulated in tensor memory between two drains into the
-// epilogue's FP32 registers (1: every 64-wide k-block; larger G drains less
-// often at a longer in-TMEM accumulation chain).
-template <int PARTS, int STAGES, int G>
-__global__ void __launch_bounds__(THREADS, 1)
+// epilogue's FP32 registers (1: every k-block; larger G drains less often at
+// a longer in-TMEM accumulation chain).
+template <int PARTS, int STAGES, int G, int BN_T>
+__global__ void __launch_bounds__(Shape<BN_T>::THREADS, 1)
 gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    float* __restrict__ P, uint32_t M, uint32_t N, uint32_t Kp, uint32_t spin_limit,
                    unsigned int* err) {
-  constexpr int STAGE_BYTES = 2 * PARTS * TILE_BYTES;
+  using SH = Shape<BN_T>;
+  constexpr int BN = SH::BN, BK = SH::BK;
+  constexpr int STAGE_BYTES = PARTS * (SH::A_TILE + SH::B_TILE);
+  constexpr uint32_t TMEM_COLS = SH::TMEM_COLS;
+  constexpr uint32_t IDESC = SH::IDESC;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
@@ -171,7 +190,8 @@ gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
     }
     for (int a = 0; a < 2; ++a) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&acc_full[a])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" :: "r"(smem_u32(&acc_empty[a])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;"
+                   :: "r"(smem_u32(&acc_empty[a])), "r"(SH::EPI_WARPS));
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&drain_bar)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -209,14 +229,14 @@ gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
           asm volatile(
               "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
               " [%0], [%1, {%2, %3, %4}], [%5];"
-              :: "r"(stage + (uint32_t)p * TILE_BYTES), "l"(&tmA), "r"(kx), "r"((int)m0), "r"(p),
+              :: "r"(stage + (uint32_t)p * SH::A_TILE), "l"(&tmA), "r"(kx), "r"((int)m0), "r"(p),
                  "r"(fb)
               : "memory");
           asm volatile(
               "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
               " [%0], [%1, {%2, %3, %4}], [%5];"
-              :: "r"(stage + (uint32_t)(PARTS + p) * TILE_BYTES), "l"(&tmB), "r"(kx), "r"((int)n0),
-                 "r"(p), "r"(fb)
+              :: "r"(stage + (uint32_t)(PARTS * SH::A_TILE + p * SH::B_TILE)), "l"(&tmB), "r"(kx),
+                 "r"((int)n0), "r"(p), "r"(fb)
               : "memory");
         }
       }
@@ -257,8 +277,9 @@ gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
         const uint32_t dtm = tmem + (uint32_t)(acc_i * BN);
 #pragma unroll
         for (int q = 0; q < NPROD; ++q) {
-          const uint64_t ad = smem_desc(stage + (uint32_t)prod_a[q] * TILE_BYTES);
-          const uint64_t bd = smem_desc(stage + (uint32_t)(PARTS + prod_b[q]) * TILE_BYTES);
+          const uint64_t ad = smem_desc<BN_T>(stage + (uint32_t)prod_a[q] * SH::A_TILE);
+          const uint64_t bd =
+              smem_desc<BN_T>(stage + (uint32_t)(PARTS * SH::A_TILE + prod_b[q] * SH::B_TILE));
 #pragma unroll
           for (int ks = 0; ks < BK / 16; ++ks) {
             // advance 16 bf16 = 32 bytes along K inside the swizzle row
@@ -288,12 +309,15 @@ gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
       if (!mbar_wait(smem_u32(&drain_bar), 0, spin_limit)) raise(err);
     }
   } else {
-    // ---- epilogue: warps 2..5 own TMEM lanes 32*(warp % 4) ...; each thread
-    //      keeps its row's 128 partial sums in registers
+    // ---- epilogue: warp w (2 .. 1 + EPI_WARPS) owns TMEM lanes 32*(w % 4) ..
+    //      and columns 128*((w - 2) / 4) ..; each thread keeps its row's 128
+    //      partial sums in registers
+    constexpr int CW = 128;  // columns per epilogue warp
     const int q = warp & 3;
-    float sum[BN];
+    const int h = (warp - 2) >> 2;
+    float sum[CW];
 #pragma unroll
-    for (int j = 0; j < BN; ++j) sum[j] = 0.0f;
+    for (int j = 0; j < CW; ++j) sum[j] = 0.0f;
     bool ok = true;
     const uint32_t ngrp = (nk + G - 1) / G;
     for (uint32_t grp = 0; grp < ngrp; ++grp) {
@@ -305,10 +329,10 @@ gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-      for (int c = 0; c < BN / 32; ++c) {
+      for (int c = 0; c < CW / 32; ++c) {
         uint32_t r[32];
         const uint32_t taddr =
-            tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc_i * BN + c * 32);
+            tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc_i * BN + h * CW + c * 32);
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10,"
             " %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27,"
@@ -337,8 +361,8 @@ gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
       if (row < M) {
         const bool vec = (N % 4u) == 0u;
 #pragma unroll
-        for (int c = 0; c < BN / 32; ++c) {
-          const uint32_t col0 = n0 + (uint32_t)(c * 32);
+        for (int c = 0; c < CW / 32; ++c) {
+          const uint32_t col0 = n0 + (uint32_t)(h * CW + c * 32);
           float* dst = P + (uint64_t)row * N + col0;
           if (vec && col0 + 32 <= N) {
 #pragma unroll
@@ -378,8 +402,8 @@ inline uint32_t round_up(uint32_t v, uint32_t m) { return (v + m - 1) / m * m; }
 }  // namespace tc
 
 size_t allpairs_tc_scratch_bytes(uint32_t M, uint32_t N, uint32_t K, int parts) {
-  const uint64_t Mp = tc::round_up(M, tc::BM), Np = tc::round_up(N, tc::BN),
-                 Kp = tc::round_up(K, tc::BK);
+  const uint64_t Mp = tc::round_up(M, tc::BM), Np = tc::round_up(N, tc::NPAD),
+                 Kp = tc::round_up(K, tc::KPAD);
   return (size_t)parts * (Mp + Np) * Kp * 2 + 1024;
 }
 
@@ -391,39 +415,43 @@ bool allpairs_tc_supported(uint32_t M, uint32_t N, uint32_t K, const void*, cons
   return (uint64_t)M * N >= 128ull * 128ull && K >= 16 && rt().cc_major == 10;
 }
 
-static int encode_parts(CUtensorMap* tm, void* base, uint64_t rows, uint64_t Kp, int parts) {
+static int encode_parts(CUtensorMap* tm, void* base, uint64_t rows, uint64_t Kp, int parts,
+                        uint32_t box_rows, uint32_t box_k) {
   cuuint64_t dims[3] = {Kp, rows, (cuuint64_t)parts};
   cuuint64_t strides[2] = {Kp * 2, rows * Kp * 2};
-  cuuint32_t box[3] = {(cuuint32_t)tc::BK, (cuuint32_t)tc::BM, 1};
+  cuuint32_t box[3] = {box_k, box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = rt().drv.cuTensorMapEncodeTiled(
       tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
-      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      CU_TENSOR_MAP_INTERLEAVE_NONE,
+      box_k == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return cu_fail(r, "cuTensorMapEncodeTiled(3xbf16 parts)");
   return SCL_OK;
 }
 
 namespace {
-template <int PARTS, int STAGES, int G>
+template <int PARTS, int STAGES, int G, int BN_T>
 cudaError_t launch_gemm(dim3 grid, cudaStream_t stream, const CUtensorMap& tmA, const CUtensorMap& tmB,
                         float* P, uint32_t M, uint32_t N, uint32_t Kp, uint32_t spin_limit,
                         unsigned int* err) {
-  const size_t smem = (size_t)STAGES * 2 * PARTS * tc::TILE_BYTES + 1024;
-  auto kern = tc::gemm_3xbf16_kernel<PARTS, STAGES, G>;
+  using SH = tc::Shape<BN_T>;
+  const size_t smem = (size_t)STAGES * PARTS * (SH::A_TILE + SH::B_TILE) + 1024;
+  auto kern = tc::gemm_3xbf16_kernel<PARTS, STAGES, G, BN_T>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kern<<<grid, tc::THREADS, smem, stream>>>(tmA, tmB, P, M, N, Kp, spin_limit, err);
+  kern<<<grid, SH::THREADS, smem, stream>>>(tmA, tmB, P, M, N, Kp, spin_limit, err);
   return cudaGetLastError();
 }
 }  // namespace
 
 int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uint32_t N,
-                       uint32_t K, int parts, int trans, int drain, void* scratch, size_t scratch_bytes,
-                       cudaStream_t stream, uint32_t spin_limit, unsigned int* err) {
+                       uint32_t K, int parts, int trans, int drain, int wide, void* scratch,
+                       size_t scratch_bytes, cudaStream_t stream, uint32_t spin_limit,
+                       unsigned int* err) {
   if (parts != 2 && parts != 3) return fail(SCL_ERR_ARG, "3xBF16: parts must be 2 or 3");
-  const uint32_t Mp = tc::round_up(M, tc::BM), Np = tc::round_up(N, tc::BN),
-                 Kp = tc::round_up(K, tc::BK);
+  const uint32_t Mp = tc::round_up(M, tc::BM), Np = tc::round_up(N, tc::NPAD),
+                 Kp = tc::round_up(K, tc::KPAD);
   if (scratch_bytes < allpairs_tc_scratch_bytes(M, N, K, parts))
     return fail(SCL_ERR_ARG, "3xBF16: scratch too small");
   uint8_t* s = reinterpret_cast<uint8_t*>(((uintptr_t)scratch + 1023) & ~(uintptr_t)1023);
@@ -449,21 +477,27 @@ int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uin
   rt().launches += 2;
 
   alignas(64) CUtensorMap tmA, tmB;
-  if (int st = encode_parts(&tmA, a_parts, Mp, Kp, parts)) return st;
-  if (int st = encode_parts(&tmB, b_parts, Np, Kp, parts)) return st;
+  const uint32_t bn = wide ? 256 : 128, bk = wide ? 32 : 64;
+  if (int st = encode_parts(&tmA, a_parts, Mp, Kp, parts, tc::BM, bk)) return st;
+  if (int st = encode_parts(&tmB, b_parts, Np, Kp, parts, bn, bk)) return st;
 
-  dim3 grid(Np / tc::BN, Mp / tc::BM);
+  dim3 grid((N + bn - 1) / bn, Mp / tc::BM);
   if (grid.y > 65535) return fail(SCL_ERR_ARG, "3xBF16: too many row tiles");
-  // parts 3: 2 stages of 96 KB; parts 2: 3 stages of 64 KB
   cudaError_t e;
-  if (parts == 3) {
-    e = drain >= 4 ? launch_gemm<3, 2, 4>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
-      : drain == 2 ? launch_gemm<3, 2, 2>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
-                   : launch_gemm<3, 2, 1>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err);
+  if (wide) {
+    // 128 x 256 tiles, k-blocks of 32: drains every 2 k-blocks (64 K, as the
+    // narrow shape's default); parts 3: 3 stages of 72 KB; parts 2: 4 of 48 KB
+    e = parts == 3 ? launch_gemm<3, 3, 2, 256>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
+                   : launch_gemm<2, 4, 2, 256>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err);
+  } else if (parts == 3) {
+    // parts 3: 2 stages of 96 KB; parts 2: 3 stages of 64 KB
+    e = drain >= 4 ? launch_gemm<3, 2, 4, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
+      : drain == 2 ? launch_gemm<3, 2, 2, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
+                   : launch_gemm<3, 2, 1, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err);
   } else {
-    e = drain >= 4 ? launch_gemm<2, 3, 4>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
-      : drain == 2 ? launch_gemm<2, 3, 2>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
-                   : launch_gemm<2, 3, 1>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err);
+    e = drain >= 4 ? launch_gemm<2, 3, 4, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
+      : drain == 2 ? launch_gemm<2, 3, 2, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
+                   : launch_gemm<2, 3, 1, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err);
   }
   if (e != cudaSuccess) return cuda_fail(e, "3xBF16 launch");
   rt().launches += 1;

@@ -12,8 +12,9 @@
 // tcgen05 contraction (allpairs_tc.cu)
 namespace scl {
 int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uint32_t N,
-                       uint32_t K, int parts, int trans, int drain, void* scratch, size_t scratch_bytes,
-                       cudaStream_t stream, uint32_t spin_limit, unsigned int* err);
+                       uint32_t K, int parts, int trans, int drain, int wide, void* scratch,
+                       size_t scratch_bytes, cudaStream_t stream, uint32_t spin_limit,
+                       unsigned int* err);
 // row-major rows x cols -> cols x rows, elements of 4 or 8 bytes (adjoint.cu)
 int transpose_launch(const void* src, void* dst, uint64_t rows, uint64_t cols, size_t elem,
                      cudaStream_t stream);
@@ -621,10 +622,18 @@ extern "C" int scl_launch_allpairs(scl_program* p, const scl_shape* sh, void* co
       const size_t need = allpairs_tc_scratch_bytes(M, N, K, parts);
       if (int st = ensure_workspace(p, need)) return st;
       p->last_variant = SCL_VARIANT_TC3XBF16;
-      // tuning.tile_w: k-blocks accumulated in tensor memory per drain (1, 2 or 4)
+      // tuning.tile_w: k-blocks accumulated in tensor memory per drain of a
+      // 128-column tile (1, 2 or 4)
       const int drain = (tu && tu->tile_w) ? (int)tu->tile_w : 1;
+      // tuning.tile_h: output-tile columns, 128 or 256 (k-blocks of 32, drained
+      // every 2); 0 takes 256 when the 128 x 256 tiles still give every SM one
+      const uint32_t cols = tu ? tu->tile_h : 0u;
+      const uint64_t wide_tiles = (uint64_t)((M + 127u) / 128u) * ((N + 255u) / 256u);
+      const uint64_t sms = rt().sm_count > 0 ? (uint64_t)rt().sm_count : 148u;
+      const int wide = cols == 256u || (cols == 0u && wide_tiles >= sms) ? 1 : 0;
       return allpairs_tc_launch((const float*)A, (const float*)B, (float*)P, M, N, K, parts, trans,
-                                drain, p->ws.ptr, p->ws.bytes, rt().stream, spin_of(tu), rt().dev_err);
+                                drain, wide, p->ws.ptr, p->ws.bytes, rt().stream, spin_of(tu),
+                                rt().dev_err);
     }
     if (want == SCL_VARIANT_TC3XBF16)
       return fail(SCL_ERR_UNSUPPORTED, "the tensor-core AllPairs needs zip x*y, reduce x+y, identity 0, "
