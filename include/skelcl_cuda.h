@@ -99,7 +99,8 @@ typedef struct scl_program_desc {
 /* Program flags. */
 #define SCL_PROG_NO_F64_CARRY 0x1u  /* keep float carries in float            */
 #define SCL_PROG_STENCIL_COLS1 0x2u /* MapOverlap: one output column per thread
-                                       (default: two, sharing their taps)     */
+                                       (default: four, sharing their taps)    */
+#define SCL_PROG_STENCIL_COLS2 0x4u /* MapOverlap: two output columns per thread */
 
 typedef struct scl_program scl_program;
 

@@ -543,8 +543,11 @@ static int launch_mapoverlap_impl(scl_program* p, const scl_shape* sh, void* con
   if (rows > 0x7fffffffull || cols > 0x7fffffffull) return fail(SCL_ERR_ARG, "matrix too large");
   const size_t tsz = p->type_sizes[0];
   const bool want_tma = !(tu && tu->variant == SCL_VARIANT_LDST);
-  int PY = (tu && tu->tile_h) ? (int)tu->tile_h : 8;  // output rows per thread
-  if (PY != 4 && PY != 8 && PY != 16) PY = 8;
+  // output rows per thread; default 16 outputs per thread (4 x 4, or 8 x 2
+  // with two columns, 8 x 1 with one)
+  const int py_default = p->stencil_px == 4 ? 4 : 8;
+  int PY = (tu && tu->tile_h) ? (int)tu->tile_h : py_default;
+  if (PY != 4 && PY != 8 && PY != 16) PY = py_default;
   const int R = p->overlap_range, TW = 32 * p->stencil_px;
   const int xal = tsz <= 16 ? (int)std::max<size_t>(1, 16 / tsz) : 1;
   const int xlead = (R + xal - 1) / xal * xal;
@@ -793,7 +796,11 @@ extern "C" int scl_launch_mapoverlap(scl_program* p, const scl_shape* sh, void* 
     return true;
   }();
   std::vector<scl_tuning> cands;
+  // four columns per thread: 16 rows would unroll 64 user calls (slow to
+  // compile, measured slower)
+  const std::vector<uint32_t> pys =
+      p->stencil_px == 4 ? std::vector<uint32_t>{4u, 8u} : std::vector<uint32_t>{4u, 8u, 16u};
   for (uint32_t v : {SCL_VARIANT_TMA, SCL_VARIANT_LDST})
-    for (uint32_t py : {4u, 8u, 16u}) cands.push_back(shape(0, 0, 0, py, v));
+    for (uint32_t py : pys) cands.push_back(shape(0, 0, 0, py, v));
   return tuned_launch(p, "mapoverlap", sh->rows * sh->cols, tu, safe, cands, run);
 }

@@ -175,7 +175,7 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
     s << "#define SCL_IDENTITY (" << (d->identity && *d->identity ? d->identity : "0") << ")\n";
   if (kind == SCL_KIND_MAPOVERLAP) {
     std::string neutral = d->neutral && *d->neutral ? d->neutral : "0";
-    p->stencil_px = (d->flags & SCL_PROG_STENCIL_COLS1) ? 1 : 2;
+    p->stencil_px = (d->flags & SCL_PROG_STENCIL_COLS1) ? 1 : ((d->flags & SCL_PROG_STENCIL_COLS2) ? 2 : 4);
     s << "#define SCL_PX " << p->stencil_px << "\n"
       << "#define SCL_OVERLAP_RANGE " << d->overlap_range << "\n"
       << "#define SCL_PADDING " << (d->padding == SCL_PAD_NEAREST ? 1 : 0) << "\n"
@@ -360,9 +360,16 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
       break;
     case SCL_KIND_MAPOVERLAP:
       s << scl_tpl_mapoverlap;
-      out->kernels = {"scl_mapoverlap_tma<8>"};
-      out->lazy = {"scl_mapoverlap_ldst<4>", "scl_mapoverlap_tma<4>", "scl_mapoverlap_ldst<8>",
-                   "scl_mapoverlap_tma<16>"};
+      // the default rows per thread: 4 with four columns, else 8
+      if (p->stencil_px == 4) {
+        out->kernels = {"scl_mapoverlap_tma<4>"};
+        out->lazy = {"scl_mapoverlap_ldst<4>", "scl_mapoverlap_tma<8>", "scl_mapoverlap_ldst<8>",
+                     "scl_mapoverlap_tma<16>"};
+      } else {
+        out->kernels = {"scl_mapoverlap_tma<8>"};
+        out->lazy = {"scl_mapoverlap_ldst<4>", "scl_mapoverlap_tma<4>", "scl_mapoverlap_ldst<8>",
+                     "scl_mapoverlap_tma<16>"};
+      }
       break;
     case SCL_KIND_ALLPAIRS:
       s << scl_tpl_allpairs;

@@ -331,6 +331,37 @@ def test_mapoverlap_gauss_fp64(scl, orc, shape, padding, variant):
     assert np.abs(got - ref).max() <= 2e-4, np.abs(got - ref).max()
 
 
+@pytest.mark.parametrize("cols_flag,py", [(S.PROG_STENCIL_COLS1, 8), (S.PROG_STENCIL_COLS2, 8),
+                                          (S.PROG_STENCIL_COLS2, 4), (0, 4), (0, 8)])
+@pytest.mark.parametrize("padding", [S.PAD_NEUTRAL, S.PAD_NEAREST])
+@pytest.mark.parametrize("variant", [S.VARIANT_TMA, S.VARIANT_LDST])
+def test_mapoverlap_thread_shapes_exact(scl, cols_flag, py, padding, variant):
+    """One, two or four output columns per thread (default four) and 4 or 8
+    rows: an asymmetric integer stencil is exact against numpy, on a ragged
+    300 x 520 matrix."""
+    rows, cols, R = 300, 520, 4
+    img = (np.arange(rows * cols, dtype=np.int64) * 7919 % 1000).astype(np.int32).reshape(rows, cols)
+    src = ("int func(input_matrix_t m){ return 3 * getData(m, -3, 2) + getData(m, 4, -1)"
+           " - getData(m, 0, -4); }")
+    p = S.Program(S.KIND_MAPOVERLAP, src, ["int", "int"], overlap_range=R, padding=padding,
+                  neutral="-5", flags=cols_flag)
+    din, dout = dev(img), S.DeviceArray(rows * cols, np.int32)
+    p.launch([din, dout], rows=rows, cols=cols, tuning=S.Tuning(variant=variant, tile_h=py))
+    assert p.last_variant == variant
+    if padding == S.PAD_NEAREST:
+        def at(dx, dy):
+            ys = np.clip(np.arange(rows) + dy, 0, rows - 1)
+            xs = np.clip(np.arange(cols) + dx, 0, cols - 1)
+            return img[ys][:, xs]
+    else:
+        pad = np.pad(img, R, constant_values=-5)
+
+        def at(dx, dy):
+            return pad[R + dy:R + dy + rows, R + dx:R + dx + cols]
+    ref = 3 * at(-3, 2) + at(4, -1) - at(0, -4)
+    assert np.array_equal(dout.to_numpy().reshape(rows, cols), ref)
+
+
 def test_mapoverlap_neutral_nonzero(scl, orc):
     rows, cols = 64, 96
     img = orc.uniform_f32(rows * cols, 9, 0.0, 1.0).reshape(rows, cols)
