@@ -127,6 +127,15 @@ int pack_extra(scl_program* p, CUfunction fn, size_t fixed, const unsigned char*
 }
 
 int launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, ArgPack& pack) {
+  // `smem` is the kernel's own dynamic shared memory; Local arguments
+  // (offsets packed from 0) follow it, 16-byte aligned
+  if (pack.nvals > 0) {
+    const size_t base = (smem + 15) & ~(size_t)15;
+    if (base + pack.local_bytes > 0xffffffffull) return fail(SCL_ERR_ARG, "Local arguments too large");
+    for (int i = 0; i < pack.nvals; ++i) pack.vals[i] += (uint32_t)base;
+    smem = base + pack.local_bytes;
+    pack.nvals = 0;  // offsets are final: a second launch of this pack keeps them
+  }
   if (smem > 32 * 1024) {  // beyond the default dynamic limit once static smem is counted
     CUresult r = rt().drv.cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
                                              (int)smem);
@@ -291,7 +300,7 @@ static int launch_map_impl(scl_program* p, const scl_shape* sh, void* const* buf
     }
     p->last_variant = SCL_VARIANT_VECTOR;
   }
-  return launch(fn, grid, block, pack.local_bytes, pack);
+  return launch(fn, grid, block, 0, pack);
 }
 
 extern "C" int scl_launch_zip(scl_program* p, const scl_shape* sh, void* const* bufs,
