@@ -153,6 +153,10 @@ namespace {
 
 int max_resident_blocks(CUfunction fn, int block, size_t smem) {
   int per_sm = 0;
+  // the query counts only what the function may use: raise its dynamic limit
+  // first, as launch() does
+  if (smem > 32 * 1024)
+    rt().drv.cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem);
   if (rt().drv.cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem) != CUDA_SUCCESS ||
       per_sm < 1)
     per_sm = 1;
