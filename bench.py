@@ -372,9 +372,16 @@ def secondary(S, oracle, hbm_peak, args):
     # Map / Zip / Reduce at 2^26 and their adjoints (the user's vector-Jacobian
     # products; the broadcast for Reduce(+))
     n = 1 << 26
-    xa = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 2, -1.0, 1.0))
-    ya = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 4, -1.0, 1.0))
-    ga = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 3, -1.0, 1.0))
+    hx, hy, hg = (oracle.uniform_f32(n, 2, -1.0, 1.0), oracle.uniform_f32(n, 4, -1.0, 1.0),
+                  oracle.uniform_f32(n, 3, -1.0, 1.0))
+    xa, ya, ga = S.DeviceArray.from_numpy(hx), S.DeviceArray.from_numpy(hy), S.DeviceArray.from_numpy(hg)
+    x64, y64, g64 = hx.astype(np.float64), hy.astype(np.float64), hg.astype(np.float64)
+
+    def rel_err(dev_arr, ref):
+        """largest element-wise relative error against the FP64 value"""
+        got = dev_arr.to_numpy().astype(np.float64)
+        den = np.abs(ref)
+        return float(np.max(np.divide(np.abs(got - ref), den, out=np.zeros_like(den), where=den > 0)))
     o1, o2 = S.DeviceArray(n, np.float32), S.DeviceArray(n, np.float32)
     mp = S.Program(S.KIND_MAP, "float func(float x){ return x*x + 1.0f; }", ["float", "float"])
     mpa = S.Program(S.KIND_MAP_ADJOINT, "float d(float x, float g){ return 2.0f*x*g; }", ["float", "float"], func="d")
@@ -392,13 +399,30 @@ def secondary(S, oracle, hbm_peak, args):
              lambda: S.check(L.scl_adjoint_broadcast(ga.ptr, o1.ptr, n, S.DTYPE_F32, 0)))):
         f_ms = timed(S, fwd_fn, 10, 3)
         a_ms = timed(S, adj_fn, 10, 3)
+        # errors against FP64: forward output, then the adjoint's
+        fwd_fn()
+        if name == "map_x*x+1":
+            errs = {"fwd": rel_err(o1, x64 * x64 + 1.0)}
+            adj_fn()
+            errs["adjoint"] = rel_err(o1, 2.0 * x64 * g64)
+        elif name == "zip_x*y":
+            errs = {"fwd": rel_err(o1, x64 * y64)}
+            adj_fn()
+            errs["adjoint_left"] = rel_err(o1, y64 * g64)
+            errs["adjoint_right"] = rel_err(o2, x64 * g64)
+        else:
+            ref = oracle.sum_f64(hx)
+            errs = {"fwd": abs(float(o2.to_numpy()[0]) - ref) / abs(ref)}
+            adj_fn()
+            errs["adjoint"] = rel_err(o1, np.full(n, g64[0]))
         adj[name] = {"fwd_GBps": round(f_bytes * n / f_ms / 1e6, 1),
                      "adjoint_GBps": round(a_bytes * n / a_ms / 1e6, 1),
                      "adjoint_frac": round(a_bytes * n / a_ms / 1e6 / hbm_peak, 3),
                      "fwd_plus_adjoint_over_fwd": round((f_ms + a_ms) / f_ms, 3),
-                     "bytes_per_elem_fwd_adjoint": [f_bytes, a_bytes]}
+                     "bytes_per_elem_fwd_adjoint": [f_bytes, a_bytes],
+                     "max_rel_err_vs_fp64": errs}
     out["elementwise_adjoints_2^26"] = adj
-    del xa, ya, ga, o1, o2
+    del xa, ya, ga, o1, o2, hx, hy, hg, x64, y64, g64
 
     # fused Map(Scan(x)) on the headline workload: the scanned vector is not written
     xs = oracle.mod_i32(N_SCAN, 0, 1001)
@@ -434,14 +458,23 @@ def secondary(S, oracle, hbm_peak, args):
         "note": "about 15 us per call is fixed (status clear, launch, ramp): 2^28 below"}
     del dxf, dg, dyf, dgx, yf, ref
     n4 = 1 << 28
-    dxf, dyf = S.DeviceArray.from_numpy(oracle.uniform_f32(n4, 2, -1.0, 1.0)), S.DeviceArray(n4, np.float32)
+    hx4 = oracle.uniform_f32(n4, 2, -1.0, 1.0)
+    dxf, dyf = S.DeviceArray.from_numpy(hx4), S.DeviceArray(n4, np.float32)
     fwd4 = timed(S, lambda: sp.launch([dxf, dyf], n=n4, flags=S.SHAPE_INCLUSIVE), 10, 3)
     bwd4 = timed(S, lambda: sp.launch([dxf, dyf], n=n4, flags=S.SHAPE_INCLUSIVE | S.SHAPE_REVERSE), 10, 3)
+    errs = {}
+    for key, rev in (("fwd", False), ("adjoint", True)):
+        sp.launch([dxf, dyf], n=n4, flags=S.SHAPE_INCLUSIVE | (S.SHAPE_REVERSE if rev else 0))
+        ref = oracle.scan_f64(hx4, inclusive=True, reverse=rev)
+        errs[key] = float(np.abs(dyf.to_numpy().astype(np.float64) - ref).max())
+        errs[key + "_max_abs_prefix"] = float(np.abs(ref).max())
+        del ref
     out["float_scan_2^28"] = {"fwd_GBps": round(8 * n4 / fwd4 / 1e6, 1),
                               "fwd_frac": round(8 * n4 / fwd4 / 1e6 / hbm_peak, 3),
                               "adjoint_GBps": round(8 * n4 / bwd4 / 1e6, 1),
-                              "fwd_plus_adjoint_over_fwd": round((fwd4 + bwd4) / fwd4, 3)}
-    del dxf, dyf
+                              "fwd_plus_adjoint_over_fwd": round((fwd4 + bwd4) / fwd4, 3),
+                              "max_abs_err_vs_fp64": errs}
+    del dxf, dyf, hx4
 
     # MapOverlap 8192^2, R = 5 Gaussian, both paddings
     rows = cols = 8192
@@ -511,16 +544,27 @@ def secondary(S, oracle, hbm_peak, args):
     res["speedup_tc6_over_simt"] = round(res["fp32_simt"]["ms"] / res["tc_3xbf16_6prod"]["ms"], 2)
     res["speedup_tc3_over_simt"] = round(res["fp32_simt"]["ms"] / res["tc_3xbf16_3prod"]["ms"], 2)
     # backward of L = sum(G * P) as two AllPairs on transposed operands (tensor cores)
-    dG = S.DeviceArray.from_numpy(oracle.normal_f32(M * N, 9))
+    hG = oracle.normal_f32(M * N, 9).reshape(M, N)
+    dG = S.DeviceArray.from_numpy(hG)
     dgA, dgB = S.DeviceArray(M * K, np.float32), S.DeviceArray(K * N, np.float32)
     f_ms = timed(S, lambda: ap.launch([dA, dB, dP], rows=M, cols=N, dim=K), 3, 1)
     a_ms = timed(S, lambda: ap.launch([dG, dB, dgA], rows=M, cols=K, dim=N, flags=S.SHAPE_TRANS_RIGHT), 3, 1)
     b_ms = timed(S, lambda: ap.launch([dA, dG, dgB], rows=K, cols=N, dim=M, flags=S.SHAPE_TRANS_LEFT), 3, 1)
+    # normwise errors against FP64 on 16 sampled rows of dA = G B^T and dB = A^T G
+    A2, B2 = A.reshape(M, K), B.reshape(K, N)
+    ra, rb = np.arange(0, M, M // 16), np.arange(0, K, K // 16)
+    ref_a = oracle.gemm_f64(np.ascontiguousarray(hG[ra]), np.ascontiguousarray(B2.T))
+    ref_b = oracle.gemm_f64(np.ascontiguousarray(A2[:, rb].T), hG)
+    got_a = dgA.to_numpy().reshape(M, K)[ra].astype(np.float64)
+    got_b = dgB.to_numpy().reshape(K, N)[rb].astype(np.float64)
     res["backward_tc_3xbf16_6prod"] = {"fwd_ms": round(f_ms, 3), "dA_ms": round(a_ms, 3), "dB_ms": round(b_ms, 3),
                                        "fwd_plus_adjoint_over_fwd": round((f_ms + a_ms + b_ms) / f_ms, 3),
+                                       "normwise_err_vs_fp64": {
+                                           "dA": float(np.abs(got_a - ref_a).max() / np.abs(ref_a).max()),
+                                           "dB": float(np.abs(got_b - ref_b).max() / np.abs(ref_b).max())},
                                        "note": "two contractions of the forward's size: 3x is the flop bound"}
     out["allpairs_8192x4096x8192"] = res
-    del dA, dB, dP, A, B, dG, dgA, dgB
+    del dA, dB, dP, A, B, dG, dgA, dgB, hG, A2, B2, ref_a, ref_b, got_a, got_b
     Ml, Kl, Nl = 4096, 256, 4096
     L_ = oracle.normal_f32(Ml * Kl, 10)
     R_ = oracle.normal_f32(Kl * Nl, 11)
@@ -528,11 +572,16 @@ def secondary(S, oracle, hbm_peak, args):
                     source2="float func(float x, float y){ return fabs(x-y); }", identity="0")
     dL, dR, dM = S.DeviceArray.from_numpy(L_), S.DeviceArray.from_numpy(R_), S.DeviceArray(Ml * Nl, np.float32)
     ms = timed(S, lambda: man.launch([dL, dR, dM], rows=Ml, cols=Nl, dim=Kl), 5, 2)
+    rm = np.arange(0, Ml, Ml // 16)
+    ref_m = oracle.manhattan_f64(np.ascontiguousarray(L_.reshape(Ml, Kl)[rm]), R_.reshape(Kl, Nl))
+    got_m = dM.to_numpy().reshape(Ml, Nl)[rm].astype(np.float64)
+    man_err = float(np.abs(got_m - ref_m).max() / np.abs(ref_m).max())
     out["segmented_10000_vectors"] = segmented(S, oracle, hbm_peak)
     out["manhattan_4096x256x4096"] = {"ms": round(ms, 3),
                                        "Gpairops": round(Ml * Nl * Kl / ms / 1e6, 1),
                                        "TFLOPs_3flop": round(3 * Ml * Nl * Kl / ms / 1e9, 2),
-                                       "fp32_frac_nominal": round(3 * Ml * Nl * Kl / ms / 1e9 / fp32_peak, 3)}
+                                       "fp32_frac_nominal": round(3 * Ml * Nl * Kl / ms / 1e9 / fp32_peak, 3),
+                                       "normwise_err_vs_fp64": man_err}
     return out
 
 
