@@ -160,8 +160,11 @@ def test_scan_adjoint_fd(scl, orc, inclusive):
 
 def test_scan_adjoint_full_size(scl, orc):
     """The float scan workload at its full size (2^26, U[-1,1]): the reverse
-    scan against the FP64 oracle."""
+    scan against the FP64 oracle, and against FP64 central differences of
+    loss = g . Scan(x) on 64 seeded coordinates (each difference runs the
+    whole FP64 forward twice)."""
     n = 1 << 26
+    x = orc.uniform_f32(n, 2, -1.0, 1.0)
     g = orc.uniform_f32(n, 3, -1.0, 1.0)
     p = S.Program(S.KIND_SCAN, ADD, ["float"], identity="0")
     dgx = S.DeviceArray(n, np.float32)
@@ -169,6 +172,20 @@ def test_scan_adjoint_full_size(scl, orc):
     got = dgx.to_numpy().astype(np.float64)
     ref = orc.scan_f64(g, inclusive=True, reverse=True)
     assert np.all(np.abs(got - ref) <= reverse_tol(n))
+    del ref
+    g64 = g.astype(np.float64)
+    loss = lambda v: float(np.dot(g64, orc.scan_f64(v, inclusive=True)))
+    for j in coords(n):
+        # in place: a copy of 2^26 floats per evaluation is not needed
+        x0 = x[j]
+        h = 1e-3 * max(1.0, abs(float(x0)))
+        x[j] = x0 + h
+        up, hp = loss(x), float(x[j])
+        x[j] = x0 - h
+        dn, hm = loss(x), float(x[j])
+        x[j] = x0
+        d = (up - dn) / (hp - hm)
+        assert abs(d - got[j]) <= 1e-4 * max(1.0, abs(got[j])), j
 
 
 # ---- MapOverlap (linear): transposed stencil ---------------------------------------------
@@ -215,6 +232,50 @@ def test_mapoverlap_adjoint(scl, orc, shape, padding):
     edge = [0, cols - 1, (rows - 1) * cols, rows * cols - 1]
     for j in list(coords(rows * cols, 60, seed=7)) + edge:
         assert abs(fd(loss, img.ravel(), j) - got.flat[j]) <= 1e-3 * max(1.0, abs(got.flat[j])), j
+
+
+@pytest.mark.parametrize("padding", [S.PAD_NEUTRAL, S.PAD_NEAREST])
+def test_mapoverlap_adjoint_full_size(scl, orc, padding):
+    """The stencil workload at its full size: 8192 x 8192 U[0,255], 11 x 11
+    Gaussian (sigma 2), loss = sum(out * w) with w U[-1,1].  The transposed
+    stencil against the FP64 oracle's adjoint, and against FP64 central
+    differences on 64 seeded pixels plus the four corners.  Moving pixel j
+    changes only the outputs within R of it, which read inputs within 2R, so
+    each difference evaluates the FP64 forward on that neighbourhood: the
+    other outputs are identical in both evaluations."""
+    rows = cols = 8192
+    R = 5
+    img = orc.uniform_f32(rows * cols, 5, 0.0, 255.0).reshape(rows, cols)
+    g = orc.uniform_f32(rows * cols, 6, -1.0, 1.0).reshape(rows, cols)
+    w = orc.gaussian_weights(R, 2.0)
+    fwd = S.Program(S.KIND_MAPOVERLAP, GAUSS_SRC, ["float", "float"], overlap_range=R,
+                    padding=padding, neutral="0")
+    got, _ = stencil_adjoint_gpu(fwd, R, g, S.buffer(dev(w)), padding)
+    ref = orc.stencil_adjoint_f64(g, R, w, padding)
+    assert np.abs(got - ref).max() <= 2e-5 * max(1.0, np.abs(ref).max())
+    del ref
+
+    def local_loss(r, c):
+        r0, r1 = max(0, r - 2 * R), min(rows, r + 2 * R + 1)
+        c0, c1 = max(0, c - 2 * R), min(cols, c + 2 * R + 1)
+        o0, o1 = max(0, r - R), min(rows, r + R + 1)
+        p0, p1 = max(0, c - R), min(cols, c + R + 1)
+        sub = np.ascontiguousarray(img[r0:r1, c0:c1])
+        gbox = g[o0:o1, p0:p1].astype(np.float64)
+
+        def loss(v):
+            # the neighbourhood's own border is an image border wherever it
+            # was clipped; elsewhere the box's outputs read only inside it
+            out = orc.stencil_f64(v.reshape(sub.shape), R, w, padding, 0.0)
+            return float((gbox * out[o0 - r0:o1 - r0, p0 - c0:p1 - c0]).sum())
+        return sub, (r - r0) * (c1 - c0) + (c - c0), loss
+
+    pix = [(int(j) // cols, int(j) % cols) for j in coords(rows * cols, 64, seed=7)]
+    pix += [(0, 0), (0, cols - 1), (rows - 1, 0), (rows - 1, cols - 1)]
+    for r, c in pix:
+        sub, j, loss = local_loss(r, c)
+        d = fd(loss, sub.ravel(), j)
+        assert abs(d - got[r, c]) <= 1e-3 * max(1.0, abs(got[r, c])), (r, c)
 
 
 # ---- AllPairs (x*y, +): two AllPairs with transposed operands -----------------------------
