@@ -17,7 +17,9 @@
 //                     element-wise adjoint kernel: d(x, g) -> dx
 //                     (dl(x, y, g) -> dx, dr(x, y, g) -> dy for Zip)
 //   Reduce (+)        a broadcast of the output gradient
+//                     (.segmented: per vector of a Segments, one launch)
 //   Scan (+)          the reverse scan of the output gradient
+//                     (.segmented: the segmented reverse scan, one launch)
 //   MapOverlap        (linear, float) the transposed stencil: the weights are
 //                     read back by running the forward on an impulse, the
 //                     adjoint is a zero-padded MapOverlap with them, plus the
@@ -39,6 +41,7 @@
 
 #include "Matrix.h"
 #include "Reduce.h"
+#include "Segments.h"
 #include "Source.h"
 #include "Vector.h"
 #include "Zip.h"
@@ -400,6 +403,44 @@ public:
     return y;
   }
 
+  // One sum per vector of `segments` (stored back to back in x), one launch;
+  // the adjoint broadcasts each vector's gradient over its elements, also in
+  // one launch.  Elements outside every vector get a zero gradient.
+  Var<Vector<T>> segmented(Tape& tape, const Var<Vector<T>>& x, const Segments& segments) const {
+    const Vector<T>& in = x.value();
+    ASSERT_MESSAGE(segments.total() <= in.size(), "ad::Reduce::segmented: segments beyond the input");
+    const size_t ns = segments.count();
+    Vector<T> o(ns);
+    if (ns > 0) {
+      void* bufs[2] = {nullptr, o.deviceOutputPtr()};
+      bufs[0] = in.size() ? (void*)in.devicePtr() : bufs[1];
+      scl_shape sh = skelcl::detail::makeShape(in.size());
+      sh.seg_offsets = segments.devicePtr();
+      sh.n_segments = ns;
+      detail::check(scl_launch_reduce(_fwd.get(), &sh, bufs, nullptr, 0, nullptr), "ad::Reduce::segmented");
+      o.dataOnDeviceModified();
+    }
+    Var<Vector<T>> y = tape.result(std::move(o), x.requiresGrad());
+    if (x.requiresGrad() && ns > 0 && in.size() > 0) {
+      auto xn = x.node();
+      auto yn = y.node();
+      const Segments segs = segments;
+      tape.record([xn, yn, segs]() {
+        if (!yn->grad) return;
+        const size_t n = xn->value->size();
+        bool acc = false;
+        void* gx = Tape::gradTarget(*xn, &acc);
+        if (!acc && segs.total() < n)
+          detail::check(scl_memset(gx, 0, n * sizeof(T)), "ad::Reduce::segmented adjoint");
+        detail::check(scl_adjoint_broadcast_segments(yn->grad->devicePtr(), gx, segs.devicePtr(), segs.count(),
+                                                     n, detail::DType<T>::value, acc ? 1 : 0),
+                      "ad::Reduce::segmented adjoint");
+        xn->grad->dataOnDeviceModified();
+      });
+    }
+    return y;
+  }
+
 private:
   skelcl::detail::Program _fwd;
 };
@@ -447,6 +488,52 @@ public:
           scl_shape s = skelcl::detail::makeShape(xn->value->size());
           s.flags = flags;
           detail::check(scl_launch_scan(prog.get(), &s, b, nullptr, 0, nullptr), "ad::Scan adjoint");
+        });
+      });
+    }
+    return y;
+  }
+
+  // One scan per vector of `segments` (stored back to back in x), one launch;
+  // the adjoint is the segmented reverse scan, also one launch.  Elements
+  // outside every vector are 0 in the result and get a zero gradient.
+  Var<Vector<T>> segmented(Tape& tape, const Var<Vector<T>>& x, const Segments& segments) const {
+    const Vector<T>& in = x.value();
+    ASSERT_MESSAGE(segments.total() <= in.size(), "ad::Scan::segmented: segments beyond the input");
+    const size_t n = in.size();
+    Vector<T> o(n);
+    if (n > 0) {
+      void* bufs[2] = {in.devicePtr(), o.deviceOutputPtr()};
+      if (segments.total() < n || segments.count() == 0)
+        detail::check(scl_memset(bufs[1], 0, n * sizeof(T)), "ad::Scan::segmented");
+      if (segments.count() > 0) {
+        scl_shape sh = skelcl::detail::makeShape(n);
+        sh.flags = _inclusive ? SCL_SHAPE_INCLUSIVE : 0u;
+        sh.seg_offsets = segments.devicePtr();
+        sh.n_segments = segments.count();
+        detail::check(scl_launch_scan(_fwd.get(), &sh, bufs, nullptr, 0, nullptr), "ad::Scan::segmented");
+      }
+      o.dataOnDeviceModified();
+    }
+    Var<Vector<T>> y = tape.result(std::move(o), x.requiresGrad());
+    if (x.requiresGrad() && n > 0) {
+      auto xn = x.node();
+      auto yn = y.node();
+      auto prog = _fwd;
+      const Segments segs = segments;
+      const uint32_t flags = SCL_SHAPE_REVERSE | (_inclusive ? SCL_SHAPE_INCLUSIVE : 0u);
+      tape.record([xn, yn, prog, segs, flags, n]() {
+        if (!yn->grad) return;
+        Tape::writeGrad(*xn, [&](void* gx) {
+          if (segs.total() < n || segs.count() == 0)
+            detail::check(scl_memset(gx, 0, n * sizeof(T)), "ad::Scan::segmented adjoint");
+          if (segs.count() == 0) return;
+          void* b[2] = {yn->grad->devicePtr(), gx};
+          scl_shape s = skelcl::detail::makeShape(n);
+          s.flags = flags;
+          s.seg_offsets = segs.devicePtr();
+          s.n_segments = segs.count();
+          detail::check(scl_launch_scan(prog.get(), &s, b, nullptr, 0, nullptr), "ad::Scan::segmented adjoint");
         });
       });
     }

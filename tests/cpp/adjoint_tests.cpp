@@ -15,6 +15,7 @@
 #include <SkelCL/MapOverlap.h>
 #include <SkelCL/Matrix.h>
 #include <SkelCL/Reduce.h>
+#include <SkelCL/Segments.h>
 #include <SkelCL/SkelCL.h>
 #include <SkelCL/Vector.h>
 #include <SkelCL/Zip.h>
@@ -105,6 +106,68 @@ TEST_F(AdjointTest, ChainMapZipScanReduce) {
   // gradients of variables add up across backward() calls; intermediates restart
   tape.backward(loss);
   for (size_t j = 0; j < n; j += 4999) EXPECT_NEAR(x.grad()[j], 2.0f * grad[j], 1e-6 * std::fabs(grad[j]));
+}
+
+// Segmented pipeline: many uneven vectors back to back (some empty, and a
+// tail outside every vector), L = sum_s gr[s] * Reduce_s(Scan_s(x*x+1)).
+TEST_F(AdjointTest, SegmentedMapScanReduce) {
+  const size_t nseg = 300;
+  std::vector<float> u = uniform(nseg, 12, 0.0f, 11.0f);
+  std::vector<size_t> lens(nseg);
+  for (size_t s = 0; s < nseg; ++s) lens[s] = s % 37 == 5 ? 0 : (size_t)std::floor(std::exp2((double)u[s]));
+  std::vector<uint64_t> off(nseg + 1, 0);
+  for (size_t s = 0; s < nseg; ++s) off[s + 1] = off[s] + lens[s];
+  const size_t total = off[nseg], n = total + 777;  // 777 elements in no vector
+  std::vector<float> xh = uniform(n, 13, -1.0f, 1.0f), grh = uniform(nseg, 14, -1.0f, 1.0f);
+  skelcl::Vector<float> xs(xh.begin(), xh.end()), gr(grh.begin(), grh.end());
+  skelcl::Segments segs(lens);
+  skelcl::ad::Tape tape;
+  auto x = tape.variable(xs);
+  skelcl::ad::Map<float(float)> sq("float func(float x){ return x*x + 1.0f; }",
+                                   "float dfunc(float x, float g){ return 2.0f*x*g; }");
+  skelcl::ad::Scan<float> scan(kAdd);
+  scan.setInclusive(true);
+  skelcl::ad::Reduce<float> sum(kAdd);
+  auto per = sum.segmented(tape, scan.segmented(tape, sq(tape, x), segs), segs);
+  ASSERT_EQ(per.value().size(), nseg);
+  tape.backward(per, gr);
+  std::vector<float> grad(x.grad().begin(), x.grad().end());
+
+  // the same gradient from forward skeletons: element i of vector s gets
+  // gr[s] * (off[s+1] - i) * 2 x_i, found by a Map over indices
+  skelcl::Vector<uint64_t> offv(off.begin(), off.end());
+  skelcl::Map<float(skelcl::Index)> weight(
+      "float func(Index i, __global const ulong* off, unsigned int ns, __global const float* gr) {"
+      "  if (i >= off[ns]) return 0.0f;"
+      "  unsigned int lo = 0, hi = ns - 1;"
+      "  while (lo < hi) { unsigned int mid = (lo + hi + 1) / 2; if (off[mid] <= i) lo = mid; else hi = mid - 1; }"
+      "  while (off[lo + 1] <= i) ++lo;"
+      "  return gr[lo] * (float)(off[lo + 1] - i); }");
+  skelcl::Vector<float> gz = weight(skelcl::IndexVector(n), offv, (unsigned int)nseg, gr);
+  skelcl::Zip<float(float, float)> chain("float func(float x, float g){ return 2.0f * x * g; }");
+  skelcl::Vector<float> composed = chain(xs, gz);
+
+  auto forward = [&](const std::vector<float>& v) {  // FP64 forward
+    double l = 0.0;
+    for (size_t s = 0; s < nseg; ++s) {
+      double acc = 0.0, red = 0.0;
+      for (uint64_t i = off[s]; i < off[s + 1]; ++i) {
+        acc += (double)v[i] * v[i] + 1.0;
+        red += acc;
+      }
+      l += (double)grh[s] * red;
+    }
+    return l;
+  };
+  size_t seg = 0;
+  for (size_t j = 0; j < n; j += 613) {
+    while (seg < nseg && off[seg + 1] <= j) ++seg;
+    const double want = j < total ? 2.0 * xh[j] * grh[seg] * (double)(off[seg + 1] - j) : 0.0;
+    EXPECT_NEAR(grad[j], want, 1e-5 * std::fabs(want) + 1e-5);
+    EXPECT_NEAR(grad[j], composed[j], 1e-6 * std::fabs(want) + 1e-5);
+    EXPECT_NEAR(centralDifference(forward, xh, j), grad[j], 1e-3 * std::fabs(want) + 1e-3);
+  }
+  for (size_t j = total; j < n; ++j) EXPECT_EQ(grad[j], 0.0f);
 }
 
 TEST_F(AdjointTest, ConstantsGetNoGradient) {
