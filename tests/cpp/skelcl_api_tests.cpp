@@ -516,6 +516,122 @@ TEST_F(SkelCLTest, VectorCoherence) {  // host writes after a device pass need d
   EXPECT_EQ(42, copy[0]);
 }
 
+// ---- further restated cases ---------------------------------------------------------
+TEST_F(SkelCLTest, MapLargeHostFilledInput) {  // MapTests.cpp TempInputVector
+  skelcl::Map<float(float)> neg("float func(float f) { return -f; }");
+  skelcl::Vector<float> in(1024 * 1000);
+  for (size_t i = 0; i < in.size(); ++i) in[i] = 2.5f * (float)i;
+  skelcl::Vector<float> out;
+  out = neg(in);
+  ASSERT_EQ(in.size(), out.size());
+  for (size_t i = 0; i < out.size(); i += 997) EXPECT_EQ(-in[i], out[i]);
+  EXPECT_EQ(-in[in.size() - 1], out[out.size() - 1]);
+}
+
+TEST_F(SkelCLTest, MapMatrixScalarArgs) {  // MapTests.cpp MatrixAddArgs
+  skelcl::Map<float(float)> m("float func(float v, float a, float b) { return v + a + b; }");
+  std::vector<float> flat(10);
+  for (size_t i = 0; i < flat.size(); ++i) flat[i] = 2.5f * (float)i;
+  skelcl::Matrix<float> in(flat, 3);  // 4 rows of 3, the last row padded
+  EXPECT_EQ(skelcl::Matrix<float>::size_type(4, 3), in.size());
+  skelcl::Matrix<float> out = m(in, 5.25f, 7.75f);
+  EXPECT_EQ(in.size(), out.size());
+  for (size_t r = 0; r < out.rowCount(); ++r)
+    for (size_t c = 0; c < out.columnCount(); ++c) EXPECT_EQ(in({r, c}) + 5.25f + 7.75f, out({r, c}));
+}
+
+TEST_F(SkelCLTest, TwoDeviceRequestRunsOnOne) {  // MapTests.cpp SimpleMultiDeviceMap2
+  skelcl::terminate();
+  skelcl::init(skelcl::nDevices(2));  // one GPU: every element on device 0
+  skelcl::Map<int(float)> m("int func(float f) { return skelcl_get_device_id(); }");
+  skelcl::Vector<float> in(10);
+  skelcl::Vector<int> out = m(in);
+  ASSERT_EQ(10u, out.size());
+  for (size_t i = 0; i < out.size(); ++i) EXPECT_EQ(0, out[i]);
+}
+
+TEST_F(SkelCLTest, ReduceGrowingVector) {  // ReduceTests.cpp nSizesReduce2
+  skelcl::Reduce<float(float)> sum("float func(float x, float y){ return x+y; }");
+  skelcl::Vector<float> in;
+  skelcl::Vector<float> out;
+  for (int n = 8192; n < 8192 + 256; ++n) {
+    in.resize(n, 1.0f);
+    out = sum(in);
+    EXPECT_EQ((float)in.size(), out[0]);
+  }
+}
+
+TEST_F(SkelCLTest, VectorCopyIsDeep) {  // VectorTests.cpp Copy, CopyWithDataOnDevice
+  skelcl::Vector<int> a(5);
+  for (size_t i = 0; i < 5; ++i) a[i] = 5;
+  skelcl::Vector<int> b(a);
+  for (size_t i = 0; i < 5; ++i) a[i] = 0;
+  for (size_t i = 0; i < 5; ++i) EXPECT_EQ(5, b[i]);
+  // the same when the newest data is on the device
+  skelcl::Vector<int> c(5);
+  for (size_t i = 0; i < 5; ++i) c[i] = 5;
+  c.setDistribution(skelcl::detail::SingleDistribution<skelcl::Vector<int>>());
+  c.createDeviceBuffers();
+  c.copyDataToDevices();
+  c.dataOnDeviceModified();
+  skelcl::Vector<int> d(c);
+  for (size_t i = 0; i < 5; ++i) c[i] = 0;
+  ASSERT_EQ(5u, d.size());
+  for (size_t i = 0; i < 5; ++i) EXPECT_EQ(5, d[i]);
+}
+
+TEST_F(SkelCLTest, VectorResizeOperations) {  // VectorTests.cpp Resize
+  skelcl::Vector<int> v;
+  v.resize(10);
+  EXPECT_EQ(10u, v.size());
+  v.push_back(5);
+  EXPECT_EQ(11u, v.size());
+  v.pop_back();
+  EXPECT_EQ(10u, v.size());
+  v.insert(v.begin(), 5);
+  EXPECT_EQ(11u, v.size());
+  v.insert(v.begin(), 2, 5);
+  EXPECT_EQ(13u, v.size());
+  std::vector<int> two(2);
+  v.insert(v.begin(), two.begin(), two.end());
+  EXPECT_EQ(15u, v.size());
+  v.erase(v.begin());
+  EXPECT_EQ(14u, v.size());
+  v.erase(v.begin(), v.begin() + 2);
+  EXPECT_EQ(12u, v.size());
+  v.clear();
+  EXPECT_EQ(0u, v.size());
+}
+
+namespace {
+struct GridPoint {  // a user struct stored in a Vector
+  int x = 0, y = 0;
+  GridPoint() = default;
+  GridPoint(int x_, int y_) : x(x_), y(y_) {}
+};
+}  // namespace
+
+TEST_F(SkelCLTest, VectorOfStructsFilledThroughIterators) {  // VectorTests.cpp CompleteInitialization
+  skelcl::Vector<GridPoint> pts(1024 * 768);
+  auto it = pts.begin();
+  for (int x = 0; x < 1024; ++x)
+    for (int y = 0; y < 768; ++y) *(it++) = GridPoint(x, y);
+  EXPECT_EQ(1024u * 768u, pts.size());
+  EXPECT_EQ(23, pts[23 * 768 + 42].x);
+  EXPECT_EQ(42, pts[23 * 768 + 42].y);
+}
+
+TEST_F(SkelCLTest, MatrixFromNestedVectors) {  // MatrixTests.cpp CreateMatrixFrom2DVector
+  std::vector<std::vector<int>> rows(10, std::vector<int>(10));
+  for (int i = 0; i < 10; ++i)
+    for (int j = 0; j < 10; ++j) rows[i][j] = i * j;
+  skelcl::Matrix<int> m = skelcl::Matrix<int>::from2DVector(rows);
+  EXPECT_FALSE(m.empty());
+  EXPECT_EQ(100u, m.size().elemCount());
+  for (size_t i = 0; i < 10; ++i)
+    for (size_t j = 0; j < 10; ++j) EXPECT_EQ((int)(i * j), m[i][j]);
+}
+
 int main(int argc, char** argv) {
   ::testing::InitGoogleTest(&argc, argv);
   return RUN_ALL_TESTS();
