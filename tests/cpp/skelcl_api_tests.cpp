@@ -632,6 +632,49 @@ TEST_F(SkelCLTest, MatrixFromNestedVectors) {  // MatrixTests.cpp CreateMatrixFr
     for (size_t j = 0; j < 10; ++j) EXPECT_EQ((int)(i * j), m[i][j]);
 }
 
+// ---- distributions (test/DistributionTests.cpp): one GPU, every kind valid
+//      and placed on the one device of the global list ----------------------------
+template <typename C>
+static void expectOnTheDevice(const C& c) {
+  auto& dist = c.distribution();
+  EXPECT_TRUE(dist.isValid());
+  ASSERT_EQ(skelcl::detail::globalDeviceList.size(), dist.devices().size());
+  EXPECT_EQ(1u, dist.devices().size());
+  EXPECT_EQ(skelcl::detail::globalDeviceList[0].get(), dist.device(0).get());
+}
+
+TEST_F(SkelCLTest, DistributionKinds) {  // DistributionTests.cpp Default, Single*, Block*, Copy*
+  EXPECT_FALSE((skelcl::detail::Distribution<skelcl::Vector<int>>().isValid()));
+  skelcl::Vector<int> v1, v2, v3, v4, v5, v6;
+  v1.setDistribution(skelcl::distribution::Single(v1));
+  skelcl::distribution::setSingle(v2);
+  v3.setDistribution(skelcl::distribution::Block(v3));
+  skelcl::distribution::setBlock(v4);
+  v5.setDistribution(skelcl::distribution::Copy(v5));
+  skelcl::distribution::setCopy(v6);
+  for (auto* v : {&v1, &v2, &v3, &v4, &v5, &v6}) expectOnTheDevice(*v);
+  skelcl::Matrix<int> m1, m2, m3;
+  m1.setDistribution(skelcl::distribution::Single(m1));
+  skelcl::distribution::setBlock(m2);
+  skelcl::distribution::setCopy(m3);
+  for (auto* m : {&m1, &m2, &m3}) expectOnTheDevice(*m);
+  skelcl::IndexVector iv(1024);
+  skelcl::distribution::setSingle(iv);
+  expectOnTheDevice(iv);
+  // a skeleton still computes the whole container under each kind
+  skelcl::Map<int(int)> neg("int func(int i) { return -i; }");
+  for (int kind = 0; kind < 3; ++kind) {
+    skelcl::Vector<int> in(1000);
+    for (size_t i = 0; i < in.size(); ++i) in[i] = (int)i;
+    if (kind == 0) skelcl::distribution::setSingle(in);
+    if (kind == 1) skelcl::distribution::setBlock(in);
+    if (kind == 2) skelcl::distribution::setCopy(in);
+    skelcl::Vector<int> out = neg(in);
+    ASSERT_EQ(in.size(), out.size());
+    for (size_t i = 0; i < out.size(); ++i) EXPECT_EQ(-(int)i, out[i]);
+  }
+}
+
 int main(int argc, char** argv) {
   ::testing::InitGoogleTest(&argc, argv);
   return RUN_ALL_TESTS();
