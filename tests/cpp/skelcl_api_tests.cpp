@@ -632,6 +632,53 @@ TEST_F(SkelCLTest, MatrixFromNestedVectors) {  // MatrixTests.cpp CreateMatrixFr
     for (size_t j = 0; j < 10; ++j) EXPECT_EQ((int)(i * j), m[i][j]);
 }
 
+namespace {
+struct Tagged {  // a user struct with a non-zero default
+  int a;
+  explicit Tagged(int v = 7) : a(v) {}
+};
+}  // namespace
+
+// VectorTests.cpp CreateEmptyVector, CreateVector; MatrixTests.cpp
+// CreateEmptyMatrix, CreateMatrix; ZipTests.cpp CreateZipWithFile; the
+// Create* cases of the skeleton suites (construction from strings and files)
+TEST_F(SkelCLTest, ContainerAndSkeletonConstruction) {
+  skelcl::Vector<int> empty;
+  EXPECT_TRUE(empty.empty());
+  EXPECT_EQ(0u, empty.size());
+  skelcl::Vector<int> zeros(10);
+  EXPECT_FALSE(zeros.empty());
+  EXPECT_EQ(10u, zeros.size());
+  for (size_t i = 0; i < zeros.size(); ++i) EXPECT_EQ(0, zeros[i]);
+  skelcl::Vector<Tagged> tagged(5, Tagged(1));
+  EXPECT_EQ(5u, tagged.size());
+  EXPECT_EQ(1, tagged.begin()->a);
+  skelcl::Matrix<int> emptyM;
+  EXPECT_TRUE(emptyM.empty());
+  skelcl::Matrix<double> md({10, 10});
+  EXPECT_FALSE(md.empty());
+  EXPECT_EQ(100u, md.size().elemCount());
+  for (size_t i = 0; i < 10; ++i)
+    for (size_t j = 0; j < 10; ++j) EXPECT_EQ(0.0, md({i, j}));
+
+  const char* fn = "skelcl_zip_function.cl";
+  { std::ofstream f(fn, std::ios_base::trunc); f << "float func(float x, float y) { return x+y; }"; }
+  std::ifstream file(fn);
+  skelcl::Zip<float(float, float)> add(file);
+  std::remove(fn);
+  skelcl::Vector<float> a(4, 1.5f), b(4, 2.0f);
+  skelcl::Vector<float> c = add(a, b);
+  for (size_t i = 0; i < 4; ++i) EXPECT_EQ(3.5f, c[i]);
+
+  skelcl::Reduce<float(float)> r("float func(float x, float y){ return x+y; }");
+  skelcl::Scan<int(int)> sc("int func(int x, int y){ return x+y; }");
+  skelcl::MapOverlap<float(float)> mo("float func(input_matrix_t f) { return -getData(f, 0, 0); }", 1);
+  skelcl::Reduce<float(float)> ar("float func(float x, float y){ return x+y; }");
+  skelcl::Zip<float(float, float)> az("float func(float x, float y){ return x*y; }");
+  skelcl::AllPairs<float(float, float)> ap(ar, az);
+  EXPECT_EQ(std::string("func"), r.func());
+}
+
 // ---- distributions (test/DistributionTests.cpp): one GPU, every kind valid
 //      and placed on the one device of the global list ----------------------------
 template <typename C>
