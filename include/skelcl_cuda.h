@@ -116,9 +116,12 @@ typedef struct scl_shape {
                             [seg_offsets[s], seg_offsets[s+1]) of the flat
                             vector of n elements.  Scan: one scan per segment;
                             Reduce: out gets n_segments results (SCL_IDENTITY
-                            for an empty segment); both in one launch after a
-                            small pre-pass.  Offsets must be non-decreasing and
-                            at most n (they are clamped, and the next
+                            for an empty segment); a small pre-pass, then one
+                            launch for the segments of up to 4096 elements
+                            (a warp each) and one for the longer ones (tiles).
+                            Offsets must be non-decreasing and at most n
+                            (otherwise they are clamped to n, a segment whose
+                            end lies before its start is empty, and the next
                             scl_sync reports SCL_ERR_ARG).  Map/Zip are
                             element-wise: segments do not change them.  No
                             counterpart in the reference.                     */

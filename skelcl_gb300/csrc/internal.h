@@ -159,12 +159,17 @@ int launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, ArgPack& pack);
 // Device status word bits (bit 0: a bounded wait gave up, set by the
 // generated kernels).
 constexpr unsigned int kDevErrSegments = 2u;  // segment offsets decreasing or past the end
-// Pre-pass of segmented launches (segments.cu): sanitised offsets and the
-// first tile of every segment (tile_start[n_seg] = tile count); tiles of
-// `tile` elements laid on the grid {a + k*vg} (vg = 1: from the segment start).
+// Pre-pass of segmented launches (segments.cu): clamped offsets (segment s
+// is read as [off[s], max(off[s], off[s+1]))) and the first tile of every
+// segment longer than short_max (tile_start[n_seg] = tile count; shorter ones
+// get none); tiles of `tile` elements laid on the grid {a + k*vg} (vg = 1:
+// from the segment start).  `scratch` holds segments_prepare_scratch(n_seg)
+// bytes.
+constexpr uint64_t kSegShort = 4096;  // longest segment one warp handles
+size_t segments_prepare_scratch(uint64_t n_seg);
 int segments_prepare(const uint64_t* seg_offsets, uint64_t n_seg, uint64_t n_total, uint64_t tile,
-                     uint64_t vg, uint64_t a, int reverse, uint64_t* off_out,
-                     unsigned int* tile_start, cudaStream_t stream);
+                     uint64_t vg, uint64_t a, int reverse, uint64_t short_max, uint64_t* off_out,
+                     unsigned int* tile_start, uint64_t* scratch, cudaStream_t stream);
 // Autotuner (tune.cpp): lookup/store of the (device, program, skeleton, size
 // bucket) cache, and the launch wrapper that times `cands` on a miss.
 bool tune_lookup(const std::string& key, scl_tuning* out);

@@ -336,24 +336,43 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
     // streams of loads (tuning.items = 8: 32 KB tiles)
     const uint32_t R = (tu && tu->items == 8) ? 8 : 32;
     const uint64_t tile = (uint64_t)R * 256 * V;
-    const uint64_t tiles = (n + tile - 1) / tile + n_seg;
+    // tiles exist only for segments longer than kSegShort (ceil(len / tile)
+    // each): at most n / tile + 1 per such segment
+    const uint64_t n_long = std::min<uint64_t>(n_seg, n / (kSegShort + 1) + 1);
+    const uint64_t tiles = (n + tile - 1) / tile + n_long;
     if (tiles > 0x7fffffffull) return fail(SCL_ERR_ARG, "segmented reduce: too many tiles");
     const std::string kname = "scl_reduce_seg<" + std::to_string(R) + ">";
     CUfunction fn = find_kernel(p, kname);
     if (!fn) return fail(SCL_ERR_LAUNCH, "kernel " + kname + " missing");
+    CUfunction fn_short = find_kernel(p, "scl_reduce_short<8>");
+    if (!fn_short) return fail(SCL_ERR_LAUNCH, "kernel scl_reduce_short<8> missing");
     auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-    const size_t tk = up(n_seg * 4), pa = up(tiles * csz), of = up((n_seg + 1) * 8);
-    if (int st = ensure_workspace(p, tk + pa + of + up((n_seg + 1) * 4))) return st;
+    const size_t tk = up(n_seg * 4), pa = up(tiles * csz), of = up((n_seg + 1) * 8),
+                 ts = up((n_seg + 1) * 4);
+    if (int st = ensure_workspace(p, tk + pa + of + ts + up(segments_prepare_scratch(n_seg)))) return st;
     char* ws = static_cast<char*>(p->ws.ptr);
     void* tickets = ws;
     void* partials = ws + tk;
     void* offs = ws + tk + pa;
     void* tstart = ws + tk + pa + of;
+    uint64_t* scratch = reinterpret_cast<uint64_t*>(ws + tk + pa + of + ts);
     SCL_CUDA(cudaMemsetAsync(tickets, 0, tk, rt().stream));
-    if (int st = segments_prepare(sh->seg_offsets, n_seg, n, tile, 1, 0, 0, (uint64_t*)offs,
-                                  (unsigned int*)tstart, rt().stream))
+    uint64_t short_max = kSegShort;
+    if (int st = segments_prepare(sh->seg_offsets, n_seg, n, tile, 1, 0, 0, short_max, (uint64_t*)offs,
+                                  (unsigned int*)tstart, scratch, rt().stream))
       return st;
     unsigned int* err = rt().dev_err;
+    // segments of at most kSegShort elements (empty ones included): one warp each
+    ArgPack spack;
+    spack.ptrs = {&in, &out, &offs, &n_seg, &short_max};
+    if (int st = pack_extra(p, fn_short, spack.ptrs.size(), (const unsigned char*)extra, extra_bytes,
+                            &spack))
+      return st;
+    uint64_t sblocks = (n_seg + 7) / 8;  // 8 warps per block
+    const uint64_t smax = (uint64_t)max_resident_blocks(fn_short, 256, spack.local_bytes);
+    if (sblocks > smax) sblocks = smax;
+    if (int st = launch(fn_short, dim3((unsigned)sblocks), dim3(256), 0, spack)) return st;
+    // longer segments: tiles (blocks past the last tile return at once)
     ArgPack pack;
     pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err};
     if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
@@ -472,7 +491,10 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   const uint64_t ga = grid ? ((16u - (reinterpret_cast<uintptr_t>(in) & 15u)) & 15u) / tsz : 0;
   uint64_t tiles;
   if (n_seg) {
-    tiles = (n + tile - 1) / tile + 2 * n_seg;  // an upper bound; the pre-pass has the count
+    // an upper bound (the pre-pass has the count): tiles exist only for
+    // segments longer than kSegShort, at most n / tile + 2 per such segment
+    const uint64_t n_long = std::min<uint64_t>(n_seg, n / (kSegShort + 1) + 1);
+    tiles = (n + tile - 1) / tile + 2 * n_long;
   } else if (staged) {
     const uint64_t m = reverse ? (ga + vg - n % vg) % vg : (vg - ga) % vg;
     tiles = (n + m + tile - 1) / tile;
@@ -503,19 +525,21 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
     void* agg;
     void* incl;
   } sargs = {nullptr, nullptr, nullptr, nullptr};
-  // segmented launches add [sanitised offsets | tile numbering] after the status
+  // segmented launches add [clamped offsets | tile numbering | pre-pass
+  // scratch] after the status
   size_t clear_bytes, total;
-  const size_t seg_of = n_seg ? up((n_seg + 1) * 8) : 0, seg_ts = n_seg ? up((n_seg + 1) * 4) : 0;
+  const size_t seg_of = n_seg ? up((n_seg + 1) * 8) : 0, seg_ts = n_seg ? up((n_seg + 1) * 4) : 0,
+               seg_sc = n_seg ? up(segments_prepare_scratch(n_seg)) : 0;
   if (p->status_mode != 0) {
     clear_bytes = 256 + up(tiles * 128);  // one 128-byte line per tile slot
     total = clear_bytes;
-    if (int st = ensure_workspace(p, total + seg_of + seg_ts)) return st;
+    if (int st = ensure_workspace(p, total + seg_of + seg_ts + seg_sc)) return st;
     sargs.slots = (char*)p->ws.ptr + 256;
   } else {
     const size_t fl = up(tiles * 4), vals = up(tiles * csz);
     clear_bytes = 256 + fl;
     total = clear_bytes + 2 * vals;
-    if (int st = ensure_workspace(p, total + seg_of + seg_ts)) return st;
+    if (int st = ensure_workspace(p, total + seg_of + seg_ts + seg_sc)) return st;
     sargs.flags = (char*)p->ws.ptr + 256;
     sargs.agg = (char*)p->ws.ptr + 256 + fl;
     sargs.incl = (char*)p->ws.ptr + 256 + fl + vals;
@@ -525,9 +549,23 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   void* tile_start = n_seg ? (char*)p->ws.ptr + total + seg_of : nullptr;
   SCL_CUDA(cudaMemsetAsync(p->ws.ptr, 0, clear_bytes, rt().stream));
   if (n_seg) {
-    if (int st = segments_prepare(sh->seg_offsets, n_seg, n, tile, vg, ga, reverse ? 1 : 0,
-                                  (uint64_t*)seg_off, (unsigned int*)tile_start, rt().stream))
+    uint64_t short_max = kSegShort;
+    uint64_t* scratch = reinterpret_cast<uint64_t*>((char*)p->ws.ptr + total + seg_of + seg_ts);
+    if (int st = segments_prepare(sh->seg_offsets, n_seg, n, tile, vg, ga, reverse ? 1 : 0, short_max,
+                                  (uint64_t*)seg_off, (unsigned int*)tile_start, scratch, rt().stream))
       return st;
+    // segments of at most kSegShort elements: one warp each
+    CUfunction fn_short = find_kernel(p, "scl_scan_short<8>");
+    if (!fn_short) return fail(SCL_ERR_LAUNCH, "kernel scl_scan_short<8> missing");
+    ArgPack spack;
+    spack.ptrs = {&in, &out, &seg_off, &n_seg, &flags, &short_max};
+    if (int st = pack_extra(p, fn_short, spack.ptrs.size(), (const unsigned char*)extra, extra_bytes,
+                            &spack))
+      return st;
+    uint64_t sblocks = (n_seg + 7) / 8;  // 8 warps per block
+    const uint64_t smax = (uint64_t)max_resident_blocks(fn_short, 256, spack.local_bytes);
+    if (sblocks > smax) sblocks = smax;
+    if (int st = launch(fn_short, dim3((unsigned)sblocks), dim3(256), 0, spack)) return st;
   }
   unsigned int spin = spin_of(tu);
   unsigned int* err = rt().dev_err;

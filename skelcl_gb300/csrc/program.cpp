@@ -338,7 +338,7 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
     case SCL_KIND_REDUCE:
       s << scl_tpl_reduce;
       out->kernels = {"scl_reduce_k<1>", "scl_reduce_k<2>", "scl_reduce_k<4>"};
-      out->lazy = {"scl_reduce_seg<32>", "scl_reduce_seg<8>"};
+      out->lazy = {"scl_reduce_seg<32>", "scl_reduce_seg<8>", "scl_reduce_short<8>"};
       break;
     case SCL_KIND_SCAN:
       s << scl_tpl_reduce << "\n" << scl_tpl_scan;
@@ -346,7 +346,8 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
       out->lazy = {"scl_scan_k<8, 3>", "scl_scan_k<8, 2>", "scl_scan_k<4, 4>", "scl_scan_k<4, 6>",
                    "scl_scan_k<2, 8>", "scl_scan_k<16, 2>", "scl_scan_k<16, 1>",
                    "scl_scan_s<8, 5>", "scl_scan_s<8, 4>", "scl_scan_s<4, 8>",
-                   "scl_scan_s<16, 3>", "scl_scan_s<8, 6, 1>", "scl_scan_s<16, 3, 1>"};
+                   "scl_scan_s<16, 3>", "scl_scan_s<8, 6, 1>", "scl_scan_s<16, 3, 1>",
+                   "scl_scan_short<8>"};
       break;
     case SCL_KIND_ZIP_REDUCE:
       s << scl_tpl_reduce;
@@ -356,7 +357,7 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
       s << scl_tpl_reduce << "\n" << scl_tpl_scan;
       out->kernels = {"scl_scan_s<8, 6>"};
       out->lazy = {"scl_scan_s<8, 5>", "scl_scan_s<8, 4>", "scl_scan_s<4, 8>", "scl_scan_s<16, 3>",
-                   "scl_scan_s<8, 6, 1>", "scl_scan_s<16, 3, 1>"};
+                   "scl_scan_s<8, 6, 1>", "scl_scan_s<16, 3, 1>", "scl_scan_short<8>"};
       break;
     case SCL_KIND_MAPOVERLAP:
       s << scl_tpl_mapoverlap;

@@ -1,16 +1,20 @@
 // Segmented launches (no counterpart in the reference): thousands of
 // vectors of uneven length stored back to back in one flat buffer, segment s
-// = [seg_offsets[s], seg_offsets[s+1]), processed by one launch per skeleton.
+// = [seg_offsets[s], seg_offsets[s+1]), processed by one launch per skeleton
+// and length class.
 //
-// segments_prepare() is the pre-pass of the segmented Scan and Reduce: it
-// copies the caller's offsets into the program workspace clamped to the
-// buffer and made non-decreasing (raising a device status bit if they were
-// not), and numbers the tiles: segment s owns tiles tile_start[s] ..
-// tile_start[s+1]-1, so no tile spans two segments: max(1, ceil(len / tile))
-// of them, or, for tiles laid on a grid of vg elements with phase a (the
-// scan's 16-byte grid), as many as cover the segment once its start (end,
-// for a reverse scan) is rounded onto the grid.  tile_start[n_segments] is
-// the tile count.
+// segments_prepare() is the pre-pass of the segmented Scan and Reduce, three
+// small launches: it copies the caller's offsets into the program workspace
+// clamped to the buffer (raising a device status bit if an offset lies past
+// the buffer or decreases; every consumer reads segment s as
+// [off[s], max(off[s], off[s+1])), so no access leaves the buffer), and
+// numbers the tiles of the segments longer than `short_max` elements:
+// segment s owns tiles tile_start[s] .. tile_start[s+1]-1, so no tile spans
+// two segments: ceil(len / tile) of them, or, for tiles laid on a grid of vg
+// elements with phase a (the scan's 16-byte grid), as many as cover the
+// segment once its start (end, for a reverse scan) is rounded onto the grid.
+// Shorter segments, empty ones included, get no tiles: one warp each handles
+// them in a separate kernel.  tile_start[n_segments] is the tile count.
 #include <cstdint>
 #include <cstring>
 
@@ -60,63 +64,98 @@ __device__ uint64_t block_incl(uint64_t v, uint64_t* s_warp) {
   return v;
 }
 
+constexpr int kSegThreads = 256, kSegPerThread = 8;
+constexpr uint64_t kSegPerBlock = (uint64_t)kSegThreads * kSegPerThread;
+
+// Tiles of a segment [lo, hi) (hi >= lo): none when it is short.
+__device__ __forceinline__ uint64_t seg_tiles(uint64_t lo, uint64_t hi, uint64_t tile, uint64_t vg,
+                                              uint64_t a, int reverse, uint64_t short_max) {
+  const uint64_t len = hi - lo;
+  if (len <= short_max) return 0;
+  // the segment's first tile starts (ends, reverse) on the grid {a + k*vg}
+  const uint64_t m = reverse ? (a + vg - hi % vg) % vg : (lo + vg - a) % vg;
+  return (len + m + tile - 1) / tile;
+}
+
+// 1. clamp the offsets, count each segment's tiles, one sum per block
+__global__ void __launch_bounds__(kSegThreads)
+seg_clamp_count_kernel(const uint64_t* off_in, uint64_t n_seg, uint64_t n_total, uint64_t tile,
+                       uint64_t vg, uint64_t a, int reverse, uint64_t short_max, uint64_t* off_out,
+                       uint64_t* block_sums, unsigned int* err) {
+  __shared__ uint64_t s_warp[32];
+  const uint64_t s0 = (uint64_t)blockIdx.x * kSegPerBlock + (uint64_t)threadIdx.x * kSegPerThread;
+  uint64_t sum = 0;
+  bool bad = false;
+#pragma unroll
+  for (int k = 0; k < kSegPerThread; ++k) {
+    const uint64_t sg = s0 + k;
+    if (sg >= n_seg) break;
+    const uint64_t rlo = off_in[sg], rhi = off_in[sg + 1];
+    bad = bad || rlo > n_total || rhi < rlo;
+    const uint64_t lo = rlo < n_total ? rlo : n_total;
+    uint64_t hi = rhi < n_total ? rhi : n_total;
+    if (hi < lo) hi = lo;
+    off_out[sg] = lo;
+    if (sg + 1 == n_seg) {
+      off_out[n_seg] = rhi < n_total ? rhi : n_total;
+      bad = bad || rhi > n_total;
+    }
+    sum += seg_tiles(lo, hi, tile, vg, a, reverse, short_max);
+  }
+  if (bad && err) atomicOr(err, kDevErrSegments);
+  const uint64_t incl = block_incl<false>(sum, s_warp);
+  if (threadIdx.x == kSegThreads - 1) block_sums[blockIdx.x] = incl;
+}
+
+// 2. exclusive sum over the blocks' sums (one block); the total at [nb]
 __global__ void __launch_bounds__(kPrepThreads)
-segments_prepare_kernel(const uint64_t* off_in, uint64_t n_seg, uint64_t n_total, uint64_t tile,
-                        uint64_t vg, uint64_t a, int reverse, uint64_t* off_out,
-                        unsigned int* tile_start, unsigned int* err) {
+seg_scan_sums_kernel(uint64_t* block_sums, uint64_t nb) {
   __shared__ uint64_t s_warp[32];
   __shared__ uint64_t s_carry;
-  __shared__ int s_bad;
-  if (threadIdx.x == 0) {
-    s_carry = 0;
-    s_bad = 0;
-  }
-  __syncthreads();
-  // 1. offsets: clamped to the buffer, running maximum
-  for (uint64_t c = 0; c <= n_seg; c += kPrepThreads) {
-    const uint64_t s = c + threadIdx.x;
-    uint64_t o = 0;
-    if (s <= n_seg) {
-      o = off_in[s];
-      if (o > n_total) {
-        o = n_total;
-        s_bad = 1;
-      }
-    }
-    uint64_t m = block_incl<true>(o, s_warp);
-    const uint64_t carry = s_carry;
-    if (carry > m) m = carry;
-    if (s <= n_seg) {
-      if (m != o) s_bad = 1;  // a decreasing offset
-      off_out[s] = m;
-    }
-    __syncthreads();
-    if (threadIdx.x == kPrepThreads - 1) s_carry = m;
-    __syncthreads();
-  }
-  // 2. tiles per segment, exclusive sum
   if (threadIdx.x == 0) s_carry = 0;
   __syncthreads();
-  for (uint64_t c = 0; c < n_seg; c += kPrepThreads) {
-    const uint64_t s = c + threadIdx.x;
-    uint64_t cnt = 0;
-    if (s < n_seg) {
-      const uint64_t lo = off_out[s], hi = off_out[s + 1];
-      // the segment's first tile starts (ends, reverse) on the grid {a + k*vg}
-      const uint64_t m = reverse ? (a + vg - hi % vg) % vg : (lo + vg - a) % vg;
-      cnt = hi == lo ? 1 : (hi - lo + m + tile - 1) / tile;
-    }
-    const uint64_t incl = block_incl<false>(cnt, s_warp);
+  for (uint64_t c = 0; c < nb; c += kPrepThreads) {
+    const uint64_t b = c + threadIdx.x;
+    const uint64_t v = b < nb ? block_sums[b] : 0;
+    const uint64_t incl = block_incl<false>(v, s_warp);
     const uint64_t carry = s_carry;
-    if (s < n_seg) tile_start[s] = (unsigned int)(carry + incl - cnt);
+    if (b < nb) block_sums[b] = carry + incl - v;
     __syncthreads();
     if (threadIdx.x == kPrepThreads - 1) s_carry = carry + incl;
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    tile_start[n_seg] = (unsigned int)s_carry;
-    if (s_bad && err) atomicOr(err, kDevErrSegments);
+  if (threadIdx.x == 0) block_sums[nb] = s_carry;
+}
+
+// 3. every segment's first tile
+__global__ void __launch_bounds__(kSegThreads)
+seg_tile_start_kernel(const uint64_t* off, uint64_t n_seg, uint64_t tile, uint64_t vg, uint64_t a,
+                      int reverse, uint64_t short_max, const uint64_t* block_sums, uint64_t nb,
+                      unsigned int* tile_start) {
+  __shared__ uint64_t s_warp[32];
+  const uint64_t s0 = (uint64_t)blockIdx.x * kSegPerBlock + (uint64_t)threadIdx.x * kSegPerThread;
+  uint64_t cnt[kSegPerThread], sum = 0;
+#pragma unroll
+  for (int k = 0; k < kSegPerThread; ++k) {
+    const uint64_t sg = s0 + k;
+    cnt[k] = 0;
+    if (sg < n_seg) {
+      const uint64_t lo = off[sg];
+      uint64_t hi = off[sg + 1];
+      if (hi < lo) hi = lo;
+      cnt[k] = seg_tiles(lo, hi, tile, vg, a, reverse, short_max);
+    }
+    sum += cnt[k];
   }
+  const uint64_t incl = block_incl<false>(sum, s_warp);
+  uint64_t start = block_sums[blockIdx.x] + incl - sum;
+#pragma unroll
+  for (int k = 0; k < kSegPerThread; ++k) {
+    const uint64_t sg = s0 + k;
+    if (sg < n_seg) tile_start[sg] = (unsigned int)start;
+    start += cnt[k];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) tile_start[n_seg] = (unsigned int)block_sums[nb];
 }
 
 // gx[i] (+)= g[s] for every element i of segment s (elements outside every
@@ -180,13 +219,23 @@ __global__ void broadcast_segments_kernel(const T* __restrict__ g, T* __restrict
 
 }  // namespace
 
+size_t segments_prepare_scratch(uint64_t n_seg) {
+  return ((n_seg + kSegPerBlock - 1) / kSegPerBlock + 1) * sizeof(uint64_t);
+}
+
 int segments_prepare(const uint64_t* seg_offsets, uint64_t n_seg, uint64_t n_total, uint64_t tile,
-                     uint64_t vg, uint64_t a, int reverse, uint64_t* off_out,
-                     unsigned int* tile_start, cudaStream_t stream) {
-  segments_prepare_kernel<<<1, kPrepThreads, 0, stream>>>(seg_offsets, n_seg, n_total, tile, vg, a,
-                                                          reverse, off_out, tile_start, rt().dev_err);
+                     uint64_t vg, uint64_t a, int reverse, uint64_t short_max, uint64_t* off_out,
+                     unsigned int* tile_start, uint64_t* scratch, cudaStream_t stream) {
+  const uint64_t nb = (n_seg + kSegPerBlock - 1) / kSegPerBlock;
+  if (nb == 0) return SCL_OK;
+  if (nb > 0x7fffffffull) return fail(SCL_ERR_ARG, "too many segments");
+  seg_clamp_count_kernel<<<(unsigned)nb, kSegThreads, 0, stream>>>(
+      seg_offsets, n_seg, n_total, tile, vg, a, reverse, short_max, off_out, scratch, rt().dev_err);
+  seg_scan_sums_kernel<<<1, kPrepThreads, 0, stream>>>(scratch, nb);
+  seg_tile_start_kernel<<<(unsigned)nb, kSegThreads, 0, stream>>>(off_out, n_seg, tile, vg, a, reverse,
+                                                                  short_max, scratch, nb, tile_start);
   SCL_CUDA(cudaGetLastError());
-  ++rt().launches;
+  rt().launches += 3;
   return SCL_OK;
 }
 

@@ -234,7 +234,7 @@ scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
   if (s_seg < 0) return;
   const scl_u64 sg = (scl_u64)s_seg;
   const unsigned int first = tile_start[sg], count = tile_start[sg + 1] - first;
-  const scl_u64 off = seg_off[sg], len = seg_off[sg + 1] - off;
+  const scl_u64 off = seg_off[sg], len = seg_off[sg + 1] > off ? seg_off[sg + 1] - off : 0;
   if (len == 0) {
     if (threadIdx.x == 0) out[sg] = (scl_T)(SCL_IDENTITY);
     return;
@@ -314,6 +314,59 @@ scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
   if (threadIdx.x == 0) {
     out[sg] = (scl_T)c;
     tickets[sg] = 0u;
+  }
+}
+
+// Segments of at most short_max elements (empty ones included: SCL_IDENTITY):
+// one warp each, grid-stride over the segments, U elements per lane in
+// flight, folded in the element type (no block boundary is crossed; FP64
+// folds here would make the FP64 pipe the bound for tiny segments); longer
+// segments are left to scl_reduce_seg.
+template <int U>
+__global__ void __launch_bounds__(256)
+scl_reduce_short(const scl_T* in, scl_T* out, const scl_u64* seg_off, scl_u64 n_seg,
+                 scl_u64 short_max SCL_EXTRA_PARAMS) {
+  SCL_EXTRA_SETUP
+  const int lane = threadIdx.x & 31;
+  const scl_u64 nw = ((scl_u64)gridDim.x * blockDim.x) >> 5;
+  scl_u64 sg = ((scl_u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // the next segment's offsets are loaded while this one is folded
+  scl_u64 lo_next = sg < n_seg ? seg_off[sg] : 0, hi_next = sg < n_seg ? seg_off[sg + 1] : 0;
+  for (; sg < n_seg; sg += nw) {
+    const scl_u64 lo = lo_next;
+    const scl_u64 len = hi_next > lo ? hi_next - lo : 0;
+    if (sg + nw < n_seg) {
+      lo_next = seg_off[sg + nw];
+      hi_next = seg_off[sg + nw + 1];
+    }
+    if (len > short_max) continue;
+    bool have = false;
+    scl_T acc;
+    for (scl_u64 b = 0; b < len; b += 32 * U) {
+      scl_T v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const scl_u64 e = b + (scl_u64)(u * 32 + lane);
+        if (e < len) v[u] = in[lo + e];
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (b + (scl_u64)(u * 32 + lane) < len) {
+          acc = have ? SCL_FUNC(acc, v[u] SCL_OP_ARGS) : v[u];
+          have = true;
+        }
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const scl_T o = scl_shfl_down(acc, off);
+      const bool oh = __shfl_down_sync(0xffffffffu, have ? 1 : 0, off) != 0;
+      if (lane + off < 32 && oh) {
+        acc = have ? SCL_FUNC(acc, o SCL_OP_ARGS) : o;
+        have = true;
+      }
+    }
+    if (lane == 0) out[sg] = have ? acc : (scl_T)(SCL_IDENTITY);
   }
 }
 #endif  // SCL_KIND == 9

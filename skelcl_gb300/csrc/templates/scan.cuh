@@ -399,6 +399,7 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
     first = tile_start[sg];
     lo = (long long)seg_off[sg];
     hi = (long long)seg_off[sg + 1];
+    if (hi < lo) hi = lo;  // a decreasing offset (reported by the pre-pass)
     if (lo == hi) return;  // an empty segment's only tile: nobody looks back at it
   }
   const long long local = (long long)(tile - first);
@@ -597,6 +598,67 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
         const long long i = tile_lo + pos + e;
         if (i >= c_lo && i < c_hi) out[i] = m.v[e];
       }
+    }
+  }
+}
+
+// Segmented scan of the segments of at most short_max elements: one warp per
+// segment, grid-stride over the segments; per round each lane scans U
+// contiguous elements serially, a warp scan combines the lanes' totals, and
+// rounds are chained through a carry in the element type (no block boundary is crossed, as inside one
+// tile of the tiled kernel; FP64 carries here would make the FP64 pipe the
+// bound for tiny segments); longer segments (and empty ones, which have
+// nothing to write) are left to scl_scan_s<R, MINB, 1>.  Operand order and
+// identity handling are those of the tiled kernel: f(earlier, later), the
+// exclusive form starts from SCL_IDENTITY.
+template <int U>
+__global__ void __launch_bounds__(256)
+scl_scan_short(const scl_T* in, scl_O* out, const scl_u64* seg_off, scl_u64 n_seg,
+               unsigned int flags, scl_u64 short_max SCL_EXTRA_PARAMS) {
+  SCL_EXTRA_SETUP
+  const int lane = threadIdx.x & 31;
+  const bool inclusive = (flags & 1u) != 0, reverse = (flags & 2u) != 0;
+  const scl_T ident = (scl_T)(SCL_IDENTITY);
+  const scl_u64 nw = ((scl_u64)gridDim.x * blockDim.x) >> 5;
+  scl_u64 sg = ((scl_u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // the next segment's offsets are loaded while this one is scanned
+  scl_u64 lo_next = sg < n_seg ? seg_off[sg] : 0, hi_next = sg < n_seg ? seg_off[sg + 1] : 0;
+  for (; sg < n_seg; sg += nw) {
+    const scl_u64 lo = lo_next;
+    const scl_u64 hi = hi_next > lo ? hi_next : lo;
+    if (sg + nw < n_seg) {
+      lo_next = seg_off[sg + nw];
+      hi_next = seg_off[sg + nw + 1];
+    }
+    const scl_u64 len = hi - lo;
+    if (len == 0 || len > short_max) continue;
+    scl_T carry = ident;
+    for (scl_u64 b = 0; b < len; b += 32 * U) {
+      // lane l owns the logical elements b + l*U .. b + l*U + U-1, which sit
+      // at lo + e, or at hi - 1 - e reversed
+      const scl_u64 e0 = b + (scl_u64)lane * U;
+      scl_T v[U];
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        const scl_u64 e = e0 + k;
+        v[k] = e < len ? in[reverse ? hi - 1 - e : lo + e] : ident;
+      }
+#pragma unroll
+      for (int k = 1; k < U; ++k) v[k] = SCL_FUNC(v[k - 1], v[k] SCL_OP_ARGS);
+      const scl_T tot = scl_warp_incl(v[U - 1] SCL_EXTRA_ARGS);
+      scl_T lane_excl = scl_shfl_up(tot, 1);
+      if (lane == 0) lane_excl = ident;
+      const scl_T pre = SCL_FUNC(carry, lane_excl SCL_OP_ARGS);
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        const scl_u64 e = e0 + k;
+        if (e < len) {
+          const scl_T r = inclusive ? SCL_FUNC(pre, v[k] SCL_OP_ARGS)
+                                    : (k == 0 ? pre : SCL_FUNC(pre, v[k - 1] SCL_OP_ARGS));
+          out[reverse ? hi - 1 - e : lo + e] = SCL_EPILOGUE(r);
+        }
+      }
+      carry = SCL_FUNC(carry, scl_shfl_idx(tot, 31) SCL_OP_ARGS);
     }
   }
 }

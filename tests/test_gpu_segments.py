@@ -56,6 +56,41 @@ def test_segmented_scan_int_exact(scl, orc, flags):
     assert np.array_equal(dy.to_numpy(), seg_scan_ref(x, off, flags))
 
 
+def mixed_offsets(seed):
+    """Mostly short vectors (a warp each), some across and past the 4096-element
+    boundary (tiles), some empty, and the boundary lengths themselves."""
+    rng = np.random.default_rng(seed)
+    short = rng.integers(0, 300, 20_000)
+    mid = rng.integers(300, 6000, 1_500)
+    long = rng.integers(6000, 40_000, 60)
+    edge = np.array([0, 1, 31, 32, 33, 255, 256, 257, 4095, 4096, 4097, 8192, 8193, 0, 0])
+    lens = np.concatenate([short, mid, long, edge])
+    rng.shuffle(lens)
+    return np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+
+
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+def test_segmented_scan_mixed_lengths_exact(scl, orc, flags):
+    off = mixed_offsets(21)
+    n = int(off[-1])
+    x = orc.mod_i32(n, 22, 1001) - 500
+    p = S.Program(S.KIND_SCAN, IADD, ["int"], identity="0")
+    dx, dy, doff = dev(x), S.DeviceArray(n, np.int32), dev(off)
+    p.launch([dx, dy], n=n, flags=flags, segments=doff)
+    assert np.array_equal(dy.to_numpy(), seg_scan_ref(x, off, flags))
+
+
+def test_segmented_reduce_mixed_lengths_exact(scl, orc):
+    off = mixed_offsets(23)
+    n = int(off[-1])
+    x = orc.mod_i32(n, 24, 1001) - 500
+    p = S.Program(S.KIND_REDUCE, IADD, ["int"], identity="0")
+    dout, doff = S.DeviceArray(len(off) - 1, np.int32), dev(off)
+    p.launch([dev(x), dout], n=n, segments=doff)
+    ref = np.bincount(seg_ids(off, n), weights=x.astype(np.float64), minlength=len(off) - 1)
+    assert np.array_equal(dout.to_numpy().astype(np.int64), ref.astype(np.int64))
+
+
 def test_segmented_scan_single_segment_equals_plain(scl, orc):
     n = 5_000_003
     x = orc.mod_i32(n, 3, 1001)
