@@ -585,6 +585,7 @@ def secondary(S, oracle, hbm_peak, args):
     gms = timed(S, lambda: gen.launch([dL, dR, dM], rows=Ml, cols=Nl, dim=Kl), 5, 2)
     got_g = dM.to_numpy().reshape(Ml, Nl)[rm].astype(np.float64)
     out["segmented_10000_vectors"] = segmented(S, oracle, hbm_peak)
+    out["segmented_1e6_short_vectors"] = segmented_short(S, oracle, hbm_peak)
     out["manhattan_4096x256x4096"] = {"ms": round(ms, 3),
                                        "Gpairops": round(Ml * Nl * Kl / ms / 1e6, 1),
                                        "TFLOPs_3flop": round(3 * Ml * Nl * Kl / ms / 1e9, 2),
@@ -596,6 +597,37 @@ def secondary(S, oracle, hbm_peak, args):
                                            "normwise_err_vs_fp64": float(np.abs(got_g - ref_m).max() /
                                                                          np.abs(ref_m).max())}}
     return out
+
+
+def segmented_short(S, oracle, hbm_peak):
+    """10^6 float32 vectors of 1..199 elements (uniform, seed 1; about 10^8
+    elements): inclusive Scan(+) and Reduce(+) per vector, one warp each, against
+    the same launches on the flat vector; the per-vector sums checked against
+    FP64 on a sample."""
+    nseg = 1_000_000
+    rng = np.random.default_rng(1)
+    lens = rng.integers(1, 200, nseg).astype(np.uint64)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+    n = int(off[-1])
+    x = oracle.uniform_f32(n, 2, -1.0, 1.0)
+    sp = S.Program(S.KIND_SCAN, "float func(float x, float y){ return x+y; }", ["float"], identity="0")
+    rp = S.Program(S.KIND_REDUCE, "float func(float x, float y){ return x+y; }", ["float"], identity="0")
+    dx, dy, dr, doff = (S.DeviceArray.from_numpy(x), S.DeviceArray(n, np.float32),
+                        S.DeviceArray(nseg, np.float32), S.DeviceArray.from_numpy(off))
+    seg_scan = timed(S, lambda: sp.launch([dx, dy], n=n, flags=S.SHAPE_INCLUSIVE, segments=doff), 10, 3)
+    seg_red = timed(S, lambda: rp.launch([dx, dr], n=n, segments=doff), 10, 3)
+    sums = dr.to_numpy().astype(np.float64)
+    pick = np.arange(0, nseg, nseg // 1000)
+    ref = np.array([oracle.sum_f64(x[int(off[i]):int(off[i + 1])]) for i in pick])
+    flat_scan = timed(S, lambda: sp.launch([dx, dy], n=n, flags=S.SHAPE_INCLUSIVE), 10, 3)
+    flat_red = timed(S, lambda: rp.launch([dx, dr], n=n), 10, 3)
+    return {"n_vectors": nseg, "elements": n,
+            "scan": {"ms": round(seg_scan, 4), "GBps": round(8 * n / seg_scan / 1e6, 1),
+                     "flat_ms": round(flat_scan, 4)},
+            "reduce": {"ms": round(seg_red, 4), "GBps": round(4 * n / seg_red / 1e6, 1),
+                       "flat_ms": round(flat_red, 4),
+                       "max_abs_err_vs_fp64_sampled": float(np.abs(sums[pick] - ref).max())},
+            "note": "vectors of up to 4096 elements take one warp each; longer ones tiles"}
 
 
 def segmented(S, oracle, hbm_peak):
