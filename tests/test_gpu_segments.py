@@ -91,6 +91,26 @@ def test_segmented_reduce_mixed_lengths_exact(scl, orc):
     assert np.array_equal(dout.to_numpy().astype(np.int64), ref.astype(np.int64))
 
 
+def test_segmented_with_extra_arguments(scl, orc):
+    """A scalar and a Local extra argument reach both the warp-per-vector and
+    the tiled kernels of a segmented Scan and Reduce."""
+    off = mixed_offsets(25)
+    n = int(off[-1])
+    x = orc.mod_i32(n, 26, 1001) - 500
+    src = ("int func(int a, int b, int scale, __local int* t) {"
+           " t[get_local_id(0)] = a; return a + b * scale; }")
+    sp = S.Program(S.KIND_SCAN, src, ["int"], identity="0")
+    rp = S.Program(S.KIND_REDUCE, src, ["int"], identity="0")
+    extra = S.value(1, np.int32) + S.local(4096)
+    dx, doff = dev(x), dev(off)
+    dy, dr = S.DeviceArray(n, np.int32), S.DeviceArray(len(off) - 1, np.int32)
+    sp.launch([dx, dy], n=n, flags=S.SHAPE_INCLUSIVE, segments=doff, extra=extra)
+    assert np.array_equal(dy.to_numpy(), seg_scan_ref(x, off, 1))
+    rp.launch([dx, dr], n=n, segments=doff, extra=extra)
+    ref = np.bincount(seg_ids(off, n), weights=x.astype(np.float64), minlength=len(off) - 1)
+    assert np.array_equal(dr.to_numpy().astype(np.int64), ref.astype(np.int64))
+
+
 def test_segmented_scan_single_segment_equals_plain(scl, orc):
     n = 5_000_003
     x = orc.mod_i32(n, 3, 1001)
