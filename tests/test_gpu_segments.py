@@ -111,6 +111,18 @@ def test_segmented_with_extra_arguments(scl, orc):
     assert np.array_equal(dr.to_numpy().astype(np.int64), ref.astype(np.int64))
 
 
+def test_segmented_reduce_all_empty(scl):
+    """Every vector empty, the flat buffer too: one identity per vector."""
+    p = S.Program(S.KIND_REDUCE, IADD, ["int"], identity="7")
+    dout = S.DeviceArray(5, np.int32)
+    dx = S.DeviceArray(1, np.int32)  # a valid pointer; no element is read
+    p.launch([dx, dout], n=0, segments=dev(np.zeros(6, np.uint64)))
+    assert list(dout.to_numpy()) == [7] * 5
+    p.launch([dx, dout], n=1, segments=dev(np.array([0, 0, 0, 0, 0, 1], np.uint64)))
+    got = dout.to_numpy()
+    assert list(got[:4]) == [7] * 4
+
+
 def test_segmented_scan_single_segment_equals_plain(scl, orc):
     n = 5_000_003
     x = orc.mod_i32(n, 3, 1001)
