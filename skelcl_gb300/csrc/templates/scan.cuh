@@ -620,46 +620,70 @@ scl_scan_short(const scl_T* in, scl_O* out, const scl_u64* seg_off, scl_u64 n_se
   const bool inclusive = (flags & 1u) != 0, reverse = (flags & 2u) != 0;
   const scl_T ident = (scl_T)(SCL_IDENTITY);
   const scl_u64 nw = ((scl_u64)gridDim.x * blockDim.x) >> 5;
-  scl_u64 sg = ((scl_u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  // the next segment's offsets are loaded while this one is scanned
-  scl_u64 lo_next = sg < n_seg ? seg_off[sg] : 0, hi_next = sg < n_seg ? seg_off[sg + 1] : 0;
-  for (; sg < n_seg; sg += nw) {
-    const scl_u64 lo = lo_next;
-    const scl_u64 hi = hi_next > lo ? hi_next : lo;
-    if (sg + nw < n_seg) {
-      lo_next = seg_off[sg + nw];
-      hi_next = seg_off[sg + nw + 1];
-    }
+  // round b of a segment [lo, hi): lane l holds the logical elements
+  // b + l*U .. b + l*U + U-1, which sit at lo + e, or at hi - 1 - e reversed
+  // (identity past the end, and nothing loaded for segments left to tiles)
+  auto load = [&](scl_T (&v)[U], scl_u64 lo, scl_u64 hi, scl_u64 b) {
     const scl_u64 len = hi - lo;
-    if (len == 0 || len > short_max) continue;
-    scl_T carry = ident;
-    for (scl_u64 b = 0; b < len; b += 32 * U) {
-      // lane l owns the logical elements b + l*U .. b + l*U + U-1, which sit
-      // at lo + e, or at hi - 1 - e reversed
-      const scl_u64 e0 = b + (scl_u64)lane * U;
-      scl_T v[U];
+    const bool mine = len <= short_max;
 #pragma unroll
-      for (int k = 0; k < U; ++k) {
-        const scl_u64 e = e0 + k;
-        v[k] = e < len ? in[reverse ? hi - 1 - e : lo + e] : ident;
-      }
-#pragma unroll
-      for (int k = 1; k < U; ++k) v[k] = SCL_FUNC(v[k - 1], v[k] SCL_OP_ARGS);
-      const scl_T tot = scl_warp_incl(v[U - 1] SCL_EXTRA_ARGS);
-      scl_T lane_excl = scl_shfl_up(tot, 1);
-      if (lane == 0) lane_excl = ident;
-      const scl_T pre = SCL_FUNC(carry, lane_excl SCL_OP_ARGS);
-#pragma unroll
-      for (int k = 0; k < U; ++k) {
-        const scl_u64 e = e0 + k;
-        if (e < len) {
-          const scl_T r = inclusive ? SCL_FUNC(pre, v[k] SCL_OP_ARGS)
-                                    : (k == 0 ? pre : SCL_FUNC(pre, v[k - 1] SCL_OP_ARGS));
-          out[reverse ? hi - 1 - e : lo + e] = SCL_EPILOGUE(r);
-        }
-      }
-      carry = SCL_FUNC(carry, scl_shfl_idx(tot, 31) SCL_OP_ARGS);
+    for (int k = 0; k < U; ++k) {
+      const scl_u64 e = b + (scl_u64)lane * U + k;
+      v[k] = (mine && e < len) ? in[reverse ? hi - 1 - e : lo + e] : ident;
     }
+  };
+  auto bounds = [&](scl_u64 sg, scl_u64* lo, scl_u64* hi) {
+    *lo = 0;
+    *hi = 0;
+    if (sg < n_seg) {
+      *lo = seg_off[sg];
+      const scl_u64 h = seg_off[sg + 1];
+      *hi = h > *lo ? h : *lo;
+    }
+  };
+  // software pipeline: the next segment's first round and the offsets of
+  // the one after are loaded while this segment is scanned
+  scl_u64 sg = ((scl_u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  scl_u64 lo, hi, lo_n, hi_n;
+  bounds(sg, &lo, &hi);
+  bounds(sg + nw, &lo_n, &hi_n);
+  scl_T v[U];
+  load(v, lo, hi, 0);
+  for (; sg < n_seg; sg += nw) {
+    scl_u64 lo_nn, hi_nn;
+    bounds(sg + 2 * nw, &lo_nn, &hi_nn);
+    scl_T vn[U];
+    load(vn, lo_n, hi_n, 0);
+    const scl_u64 len = hi - lo;
+    if (len > 0 && len <= short_max) {
+      scl_T carry = ident;
+      for (scl_u64 b = 0; b < len; b += 32 * U) {
+        if (b > 0) load(v, lo, hi, b);
+        const scl_u64 e0 = b + (scl_u64)lane * U;
+#pragma unroll
+        for (int k = 1; k < U; ++k) v[k] = SCL_FUNC(v[k - 1], v[k] SCL_OP_ARGS);
+        const scl_T tot = scl_warp_incl(v[U - 1] SCL_EXTRA_ARGS);
+        scl_T lane_excl = scl_shfl_up(tot, 1);
+        if (lane == 0) lane_excl = ident;
+        const scl_T pre = SCL_FUNC(carry, lane_excl SCL_OP_ARGS);
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+          const scl_u64 e = e0 + k;
+          if (e < len) {
+            const scl_T r = inclusive ? SCL_FUNC(pre, v[k] SCL_OP_ARGS)
+                                      : (k == 0 ? pre : SCL_FUNC(pre, v[k - 1] SCL_OP_ARGS));
+            out[reverse ? hi - 1 - e : lo + e] = SCL_EPILOGUE(r);
+          }
+        }
+        carry = SCL_FUNC(carry, scl_shfl_idx(tot, 31) SCL_OP_ARGS);
+      }
+    }
+    lo = lo_n;
+    hi = hi_n;
+    lo_n = lo_nn;
+    hi_n = hi_nn;
+#pragma unroll
+    for (int k = 0; k < U; ++k) v[k] = vn[k];
   }
 }
 #endif
