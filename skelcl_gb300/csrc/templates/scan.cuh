@@ -371,7 +371,12 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
   __shared__ scl_C s_prefix;
   const unsigned int bar_s = (unsigned int)__cvta_generic_to_shared(&bar);
   if (threadIdx.x == 0) {
-    s_tile = atomicAdd(tile_counter, 1u);
+    // segmented: the grid is an upper bound; blocks at or past the tile count
+    // take no ticket (all tickets below it go to the lower-numbered blocks,
+    // one each, in the order they start)
+    bool take = true;
+    if constexpr (SEG != 0) take = blockIdx.x < tile_start[n_seg];
+    s_tile = take ? atomicAdd(tile_counter, 1u) : 0xffffffffu;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar_s));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
