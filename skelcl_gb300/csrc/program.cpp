@@ -337,8 +337,9 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
       break;
     case SCL_KIND_REDUCE:
       s << scl_tpl_reduce;
-      out->kernels = {"scl_reduce_k<1>", "scl_reduce_k<2>", "scl_reduce_k<4>"};
-      out->lazy = {"scl_reduce_seg<32>", "scl_reduce_seg<8>", "scl_reduce_short<8>"};
+      out->kernels = {"scl_reduce_k<8>", "scl_reduce_k<4>"};
+      out->lazy = {"scl_reduce_k<1>", "scl_reduce_k<2>", "scl_reduce_seg<32>", "scl_reduce_seg<8>",
+                   "scl_reduce_short<8>"};
       break;
     case SCL_KIND_SCAN:
       s << scl_tpl_reduce << "\n" << scl_tpl_scan;
