@@ -140,10 +140,13 @@ typedef struct scl_shape {
 
 /* Launch tuning; NULL means "defaults or autotuned".  Zero fields keep their
  * default.  workgroup mirrors Skeleton::setWorkGroupSize (src/Skeleton.cpp:75-78). */
+/* Launch shape; a zero field takes the default. */
 typedef struct scl_tuning {
-  uint32_t workgroup;    /* threads per block                                 */
-  uint32_t items;        /* vector rows per thread (Map/Zip/Reduce/Scan)       */
-  uint32_t tile_w;       /* MapOverlap tile width / AllPairs tile             */
+  uint32_t workgroup;    /* threads per block (Map/Zip/Reduce)                */
+  uint32_t items;        /* 16-byte vectors per thread (Map/Zip/Reduce/Scan);
+                            AllPairs tensor cores: bf16 parts, 2 or 3          */
+  uint32_t tile_w;       /* Scan: tiles per SM; AllPairs tensor cores:
+                            k-blocks per drain of 128-column tiles (1, 2, 4)  */
   uint32_t tile_h;       /* MapOverlap rows per thread / AllPairs tile columns */
   uint32_t variant;      /* SCL_VARIANT_*                                     */
   uint32_t spin_limit;   /* bounded-wait polls before SCL_ERR_TIMEOUT, 0 = default */
