@@ -761,7 +761,7 @@ def run_reference(args):
 
 
 CASES = ("scan_int32", "map_mod", "zip_mul", "reduce_f32", "scan_f32", "mapoverlap", "allpairs_simt",
-         "allpairs_tc", "manhattan")
+         "allpairs_tc", "manhattan", "segmented_short")
 
 
 def run_case(args):
@@ -782,6 +782,22 @@ def run_case(args):
             p = S.Program(S.KIND_MAP, "int func(int x){ return x % 7919; }", ["int", "int"])
             fn = lambda: p.launch([x, y], n=n)
         nbytes = 8 * n
+    elif c == "segmented_short":
+        # n vectors of 1..199 float elements (uniform, seed 1), values
+        # U[-1,1] (seed 2): a segmented inclusive Scan(+) and Reduce(+) per step
+        rng = np.random.default_rng(1)
+        lens = rng.integers(1, 200, n).astype(np.uint64)
+        off = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+        ne = int(off[-1])
+        a = S.DeviceArray.from_numpy(oracle.uniform_f32(ne, 2, -1.0, 1.0))
+        z, r, doff = S.DeviceArray(ne, np.float32), S.DeviceArray(n, np.float32), S.DeviceArray.from_numpy(off)
+        sp = S.Program(S.KIND_SCAN, "float func(float x, float y){ return x+y; }", ["float"], identity="0")
+        rp = S.Program(S.KIND_REDUCE, "float func(float x, float y){ return x+y; }", ["float"], identity="0")
+
+        def fn():
+            sp.launch([a, z], n=ne, flags=S.SHAPE_INCLUSIVE, segments=doff)
+            rp.launch([a, r], n=ne, segments=doff)
+        nbytes = 12 * ne
     elif c in ("zip_mul", "reduce_f32", "scan_f32"):
         a = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 0, -1.0, 1.0))
         b = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 1, -1.0, 1.0))
@@ -838,7 +854,8 @@ def main():
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", choices=CASES, help="time one skeleton kernel (profiling)")
-    ap.add_argument("--n", type=int, default=1 << 26, help="--case size (elements)")
+    ap.add_argument("--n", type=int, default=1 << 26,
+                    help="--case size (elements; segmented_short: vectors)")
     args = ap.parse_args()
     if args.warmup < 1:
         args.warmup = 1
