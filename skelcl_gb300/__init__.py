@@ -29,7 +29,7 @@ SHAPE_ACCUMULATE, SHAPE_ACCUMULATE_RIGHT, SHAPE_TRANS_LEFT, SHAPE_TRANS_RIGHT = 
 DTYPE_F32, DTYPE_F64 = 1, 2
 VARIANT_AUTO, VARIANT_SIMPLE, VARIANT_VECTOR, VARIANT_SIMT, VARIANT_TC3XBF16, VARIANT_TMA, VARIANT_LDST = range(7)
 ARG_VALUE, ARG_BUFFER, ARG_MATRIX, ARG_LOCAL = 1, 2, 3, 4
-PROG_NO_F64_CARRY, PROG_STENCIL_COLS1, PROG_STENCIL_COLS2 = 1, 2, 4
+PROG_NO_F64_CARRY, PROG_STENCIL_COLS1, PROG_STENCIL_COLS2, PROG_COMPILE_ALL = 1, 2, 4, 8
 
 CL_TYPE = {
     np.dtype(np.float32): "float", np.dtype(np.float64): "double",

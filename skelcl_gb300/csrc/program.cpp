@@ -697,6 +697,7 @@ extern "C" int scl_program_compile(const scl_program_desc* desc, char* log, size
       copy_log(err, log, log_cap);
       return fail(st, err);
     }
+    if (desc->flags & SCL_PROG_COMPILE_ALL) a.kernels.insert(a.kernels.end(), a.lazy.begin(), a.lazy.end());
     st = nvrtc_compile(a, &cubin, &lowered, &nvlog);
     if (st == SCL_OK) {
       copy_log(nvlog, log, log_cap);

@@ -111,6 +111,53 @@ def test_reference_user_functions_compile(built, kind, src, types, kw):
     s.compile_only(kind, src, types, **kw)
 
 
+# Every kernel variant of each skeleton kind (those compiled on first use
+# included), so that a template error shows without a GPU.
+STENCIL3 = ("float func(input_matrix_t m, __global float* w) { float s = 0.0f;"
+            " for (int dy = -1; dy <= 1; ++dy) for (int dx = -1; dx <= 1; ++dx)"
+            "  s += getData(m, dx, dy) * w[(dy + 1) * 3 + (dx + 1)]; return s; }")
+ALL_VARIANTS = [
+    (s.KIND_MAP, "float func(float f){ return -f; }", ["float", "float"], {}),
+    (s.KIND_MAP, "int func(int i, __local int* lp) { lp[0] = i; return -lp[0]; }", ["int", "int"], {}),
+    (s.KIND_ZIP, "float func(float x, float y){ return x*y; }", ["float"] * 3, {}),
+    (s.KIND_REDUCE, "float func(float x, float y){ return x+y; }", ["float"], {"identity": "0"}),
+    (s.KIND_REDUCE, "double func(double x, double y){ return x+y; }", ["double"], {"identity": "0"}),
+    (s.KIND_REDUCE, "unsigned char func(unsigned char x, unsigned char y){ return x > y ? x : y; }",
+     ["unsigned char"], {"identity": "0"}),
+    (s.KIND_SCAN, "int func(int x, int y){ return x+y; }", ["int"], {"identity": "0"}),
+    (s.KIND_SCAN, "float func(float x, float y){ return x+y; }", ["float"], {"identity": "0"}),
+    (s.KIND_SCAN, "long func(long x, long y){ return x+y; }", ["long"], {"identity": "0"}),
+    (s.KIND_MAPOVERLAP, STENCIL3, ["float", "float"], {"overlap_range": 1}),
+    (s.KIND_MAPOVERLAP, STENCIL3, ["float", "float"], {"overlap_range": 1, "flags": s.PROG_STENCIL_COLS2}),
+    (s.KIND_MAPOVERLAP, STENCIL3, ["float", "float"], {"overlap_range": 1, "flags": s.PROG_STENCIL_COLS1}),
+    (s.KIND_MAPOVERLAP, "unsigned char func(input_matrix_t m){ return getData(m, 1, -1); }",
+     ["unsigned char", "unsigned char"], {"overlap_range": 1, "padding": s.PAD_NEAREST}),
+    (s.KIND_ALLPAIRS, "float func(float x, float y){ return x+y; }", ["float"] * 3,
+     {"source2": "float func(float x, float y){ return x*y; }", "identity": "0"}),
+    (s.KIND_ALLPAIRS, "double func(double x, double y){ return x+y; }", ["double"] * 3,
+     {"source2": "double func(double x, double y){ return fabs(x-y); }", "identity": "0"}),
+    (s.KIND_ALLPAIRS_GENERIC,
+     "float func(lmatrix_t* row, rmatrix_t* col, const unsigned int dim) { float r = 0;"
+     " for (unsigned int i = 0; i < dim; ++i) r += getElementFromRow(row, i) * getElementFromColumn(col, i);"
+     " return r; }", ["float"] * 3, {}),
+    (s.KIND_ZIP_REDUCE, "float func(float x, float y){ return x+y; }", ["float"] * 3,
+     {"source2": "float m(float x, float y){ return x*y; }", "func2": "m", "identity": "0"}),
+    (s.KIND_SCAN_MAP, "int func(int x, int y){ return x+y; }", ["int", "int"],
+     {"source2": "int m(int x){ return x % 7; }", "func2": "m", "identity": "0"}),
+    (s.KIND_MAP_ADJOINT, "float d(float x, float g){ return 2.0f*x*g; }", ["float", "float"], {"func": "d"}),
+    (s.KIND_ZIP_ADJOINT, "float dl(float x, float y, float g){ return y*g; }\n"
+                         "float dr(float x, float y, float g){ return x*g; }", ["float"] * 3,
+     {"func": "dl", "func2": "dr"}),
+]
+
+
+@pytest.mark.parametrize("kind,src,types,kw", ALL_VARIANTS)
+def test_every_kernel_variant_compiles(built, kind, src, types, kw):
+    kw = dict(kw)
+    kw["flags"] = kw.get("flags", 0) | s.PROG_COMPILE_ALL
+    s.compile_only(kind, src, types, **kw)
+
+
 def test_splice_forwards_extra_params_in_order(built):
     src = "float func(float f, float_matrix_t mat, float add2, int_matrix_t mat2, __local int* lp)" \
           "{ return f + get(mat, 1, 1) + add2 + get(mat2, 1, 2) + lp[0]; }"
