@@ -101,8 +101,8 @@ typedef struct scl_program_desc {
 #define SCL_PROG_STENCIL_COLS1 0x2u /* MapOverlap: one output column per thread
                                        (default: four, sharing their taps)    */
 #define SCL_PROG_STENCIL_COLS2 0x4u /* MapOverlap: two output columns per thread */
-#define SCL_PROG_COMPILE_ALL 0x8u   /* scl_program_compile: also every kernel
-                                       variant otherwise compiled on first use */
+#define SCL_PROG_COMPILE_ALL 0x8u   /* every kernel variant at once (build or
+                                       compile check), none on first use      */
 
 typedef struct scl_program scl_program;
 

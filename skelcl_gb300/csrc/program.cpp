@@ -645,6 +645,10 @@ extern "C" int scl_program_build(const scl_program_desc* desc, scl_program** out
       copy_log(err, log, log_cap);
       return fail(st, err);
     }
+    if (desc->flags & SCL_PROG_COMPILE_ALL) {  // every variant now, none on first use
+      a.kernels.insert(a.kernels.end(), a.lazy.begin(), a.lazy.end());
+      a.lazy.clear();
+    }
     st = compile_cached(a.source, a.kernels, &cubin, &lowered, &nvlog, &p->hash);
     if (st != SCL_OK) {
       if (f64) continue;  // retry with carries in the element type

@@ -493,3 +493,32 @@ def test_graph_capture_dot_product(scl, orc):
     ref = orc.dot_f64(x, y)
     assert abs(got - ref) <= 1e-5 * abs(ref)
     S.check(S.lib().scl_graph_destroy(g))
+
+
+def test_compile_all_builds_every_variant_up_front(scl, orc):
+    """SCL_PROG_COMPILE_ALL: the variants otherwise compiled on first use are
+    built with the program and give the same results."""
+    n = 100_003
+    x = orc.mod_i32(n, 31, 1001)
+    rp = S.Program(S.KIND_REDUCE, "int func(int a, int b){ return a + b; }", ["int"], identity="0",
+                   flags=S.PROG_COMPILE_ALL)
+    dx, dr = dev(x), S.DeviceArray(1, np.int32)
+    for items in (1, 2, 4, 8):
+        rp.launch([dx, dr], n=n, tuning=S.Tuning(items=items))
+        assert int(dr.to_numpy()[0]) == int(x.astype(np.int64).sum()), items
+    sp = S.Program(S.KIND_SCAN, "int func(int a, int b){ return a + b; }", ["int"], identity="0",
+                   flags=S.PROG_COMPILE_ALL)
+    dy = S.DeviceArray(n, np.int32)
+    for items, tile_w in ((8, 5), (16, 3), (4, 8)):
+        sp.launch([dx, dy], n=n, flags=S.SHAPE_INCLUSIVE, tuning=S.Tuning(items=items, tile_w=tile_w))
+        assert np.array_equal(dy.to_numpy(), np.cumsum(x, dtype=np.int64).astype(np.int32)), items
+    rows, cols = 200, 256
+    img = (np.arange(rows * cols, dtype=np.int64) % 977).astype(np.int32).reshape(rows, cols)
+    mo = S.Program(S.KIND_MAPOVERLAP, "int func(input_matrix_t m){ return getData(m, 1, 1) - getData(m, -1, 0); }",
+                   ["int", "int"], overlap_range=1, padding=S.PAD_NEAREST, flags=S.PROG_COMPILE_ALL)
+    din, dout = dev(img), S.DeviceArray(rows * cols, np.int32)
+    ys, xs = np.arange(rows), np.arange(cols)
+    ref = img[np.clip(ys + 1, 0, rows - 1)][:, np.clip(xs + 1, 0, cols - 1)] - img[:, np.clip(xs - 1, 0, cols - 1)]
+    for variant, py in ((S.VARIANT_TMA, 8), (S.VARIANT_TMA, 16), (S.VARIANT_LDST, 4), (S.VARIANT_LDST, 8)):
+        mo.launch([din, dout], rows=rows, cols=cols, tuning=S.Tuning(variant=variant, tile_h=py))
+        assert np.array_equal(dout.to_numpy().reshape(rows, cols), ref), (variant, py)
