@@ -19,7 +19,8 @@
 // reference keys its binary cache by util::hash of the source
 // (src/Program.cpp:62-75,136-175,252-281).  Environment switches kept from the
 // reference: SKELCL_LOAD_BINARY=YES, SKELCL_SAVE_BINARY=YES,
-// SKELCL_PRINT_BUILD_LOG=YES; SKELCL_CACHE_DIR picks the cache directory.
+// SKELCL_PRINT_BUILD_LOG=YES; SKELCL_CACHE_DIR picks the cache directory, and
+// SKELCL_COMPILE_ALL=YES compiles every kernel variant at construction.
 #include <nvrtc.h>
 
 #include <cstdio>
@@ -645,7 +646,8 @@ extern "C" int scl_program_build(const scl_program_desc* desc, scl_program** out
       copy_log(err, log, log_cap);
       return fail(st, err);
     }
-    if (desc->flags & SCL_PROG_COMPILE_ALL) {  // every variant now, none on first use
+    // every variant now, none on first use (flag, or SKELCL_COMPILE_ALL=YES)
+    if ((desc->flags & SCL_PROG_COMPILE_ALL) || env_yes("SKELCL_COMPILE_ALL")) {
       a.kernels.insert(a.kernels.end(), a.lazy.begin(), a.lazy.end());
       a.lazy.clear();
     }
