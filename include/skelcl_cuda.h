@@ -236,6 +236,19 @@ int scl_program_hash(const scl_program* prog, char* out41);
 /* Splice-only dry run: writes the generated CUDA source, compiles nothing. */
 int scl_program_source(const scl_program_desc* desc, char* out, size_t cap,
                        size_t* needed);
+/* Program binary cache: replaces Program::loadBinary / saveBinary
+ * (src/Program.cpp:136-175, 252-281) and keeps its switches:
+ * SKELCL_LOAD_BINARY=YES reuses cubins from SKELCL_CACHE_DIR (default
+ * $HOME/.cache/skelcl_gb300), SKELCL_SAVE_BINARY=YES writes them there,
+ * SKELCL_PRINT_BUILD_LOG=YES prints NVRTC's log.  A cubin is keyed by the
+ * generated source, the kernel names, the NVRTC options and version, this
+ * library's ABI version and (once scl_init has run) the device's compute
+ * capability and driver version; a file that is truncated, garbled or for
+ * another key is rejected and the program is compiled instead.  Counters
+ * since the library was loaded: NVRTC compilations, cubins loaded from
+ * disk, files rejected, files written (any pointer may be NULL). */
+int scl_cache_stats(uint64_t* nvrtc_compiles, uint64_t* disk_loads,
+                    uint64_t* disk_rejects, uint64_t* disk_saves);
 
 /* SHA-1 of arbitrary bytes as 40 hex characters + NUL (util::hash). */
 int scl_sha1_hex(const void* data, size_t bytes, char* out41);
@@ -332,6 +345,17 @@ int scl_autotune_get(int* mode);
 int scl_program_last_variant(const scl_program* prog, uint32_t* variant);
 /* Kernels this library launched since scl_init (all programs). */
 int scl_launch_count(uint64_t* count);
+/* Device allocations the library has made since scl_init (scl_alloc and its
+ * own scratch) and cubins it has loaded; for tests that check a call
+ * allocates or loads nothing.  No counterpart in the reference. */
+int scl_debug_counters(uint64_t* device_allocs, uint64_t* module_loads);
+/* FP32 peak probe (no counterpart in the reference): one launch of 16
+ * independent FMA chains per thread, `iters` rounds, 2048 threads per SM,
+ * scalar fma.rn.f32 or (packed != 0) fma.rn.f32x2; `sink` receives one float
+ * per thread (at least SMs x 2048 floats).  *flops = the launch's FP32 flop
+ * count; time it with events on the library stream. */
+int scl_debug_fp32_peak(int packed, uint32_t iters, float* sink, uint64_t sink_floats,
+                        uint64_t* flops);
 
 /* ---- CUDA graphs (no reference counterpart: skeleton sequences captured
  *      from the library stream and replayed with one launch). */

@@ -18,6 +18,7 @@ LIB_PATH = ORACLE_DIR / "liboracle.so"
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
 _SZ, _U64, _I, _D = ctypes.c_size_t, ctypes.c_uint64, ctypes.c_int, ctypes.c_double
 
 _SIG = {
@@ -36,6 +37,7 @@ _SIG = {
     "orc_scan_incl_mod_i32_mt": ([_i32p, _i32p, _SZ, ctypes.c_int32, _I], None),
     "orc_scan_incl_i32_mt": ([_i32p, _i32p, _SZ, _I], None),
     "orc_scan_f64": ([_f32p, _f64p, _SZ, _I, _I], None),
+    "orc_scan_affine_u32": ([_u32p, _u32p, _SZ, _I, _I], None),
     "orc_stencil_f64": ([_f32p, _SZ, _SZ, _I, _f32p, _I, _D, _f64p, _I], None),
     "orc_stencil_adjoint_f64": ([_f32p, _SZ, _SZ, _I, _f32p, _I, _f64p, _I], None),
     "orc_gemm_f64": ([_f32p, _f32p, _SZ, _SZ, _SZ, _f64p, _I], None),
@@ -136,6 +138,15 @@ def scan_f64(x, inclusive=False, reverse=False) -> np.ndarray:
     out = np.empty(len(x), np.float64)
     lib().orc_scan_f64(x, out, len(x), int(inclusive), int(reverse))
     return out
+
+
+def scan_affine_u32(pairs, inclusive=False, reverse=False) -> np.ndarray:
+    """Ordered scan of affine maps {a, b} (x -> a*x + b, uint32 wrapping),
+    f(earlier, later) = later after earlier; `pairs` has shape (n, 2)."""
+    p = np.ascontiguousarray(pairs, np.uint32).reshape(-1)
+    out = np.empty_like(p)
+    lib().orc_scan_affine_u32(p, out, len(p) // 2, int(inclusive), int(reverse))
+    return out.reshape(-1, 2)
 
 
 def stencil_f64(img, R: int, w, padding: int, neutral: float = 0.0, nthreads: int = 0) -> np.ndarray:

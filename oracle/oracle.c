@@ -236,6 +236,34 @@ void orc_scan_incl_i32_mt(const int32_t* in, int32_t* out, size_t n, int nthread
   orc_scan_mt(in, out, n, 0, nthreads);
 }
 
+/* Scan with a non-commutative associative operator, folded strictly in
+ * sequence order as f(earlier, later): composition of affine maps on
+ * uint32 (wrapping), element i = the map x -> a_i*x + b_i stored as
+ * {a_i, b_i}; f(p, q) = q after p = {q.a*p.a, q.a*p.b + q.b}; identity
+ * {1, 0}.  Exclusive output i folds elements before i (identity first), as
+ * ScanKernel.cl:74-196 seeds the exclusive scan with SCL_IDENTITY; with
+ * `reverse`, "earlier" means a higher index.  The reference itself is only
+ * well defined for commutative operators (ScanKernel.cl:135 and :243 call
+ * f(later, earlier), :177 f(earlier, later)); this fixes the order the
+ * GB300 kernels guarantee. */
+void orc_scan_affine_u32(const uint32_t* in, uint32_t* out, size_t n, int inclusive, int reverse) {
+  uint32_t a = 1u, b = 0u;
+  for (size_t k = 0; k < n; ++k) {
+    size_t i = reverse ? n - 1 - k : k;
+    const uint32_t qa = in[2 * i], qb = in[2 * i + 1];
+    if (!inclusive) {
+      out[2 * i] = a;
+      out[2 * i + 1] = b;
+    }
+    b = qa * b + qb;
+    a = qa * a;
+    if (inclusive) {
+      out[2 * i] = a;
+      out[2 * i + 1] = b;
+    }
+  }
+}
+
 void orc_scan_f64(const float* in, double* out, size_t n, int inclusive, int reverse) {
   double acc = 0.0;
   for (size_t k = 0; k < n; ++k) {

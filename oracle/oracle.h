@@ -51,6 +51,9 @@ void orc_scan_incl_i32(const int32_t* in, int32_t* out, size_t n);
  * for the integer scan workload */
 void orc_scan_incl_mod_i32_mt(const int32_t* in, int32_t* out, size_t n, int32_t m, int nthreads);
 void orc_scan_incl_i32_mt(const int32_t* in, int32_t* out, size_t n, int nthreads);
+/* ordered scan of a non-commutative operator: affine-map composition on
+ * uint32 pairs {a, b}, f(earlier, later), identity {1, 0} */
+void orc_scan_affine_u32(const uint32_t* in, uint32_t* out, size_t n, int inclusive, int reverse);
 /* double-precision scans of float input; reverse = from the last element */
 void orc_scan_f64(const float* in, double* out, size_t n, int inclusive, int reverse);
 

@@ -92,6 +92,7 @@ SIGNATURES = {
     "scl_program_source": ([ctypes.POINTER(ProgramDesc), ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ)], _I),
     "scl_program_last_variant": ([_VP, ctypes.POINTER(_U32)], _I),
     "scl_sha1_hex": ([_VP, _SZ, ctypes.c_char_p], _I),
+    "scl_cache_stats": ([ctypes.POINTER(ctypes.c_uint64)] * 4, _I),
     "scl_launch_map": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_zip": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_reduce": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
@@ -100,6 +101,8 @@ SIGNATURES = {
     "scl_launch_mapoverlap": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_allpairs": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_count": ([ctypes.POINTER(_U64)], _I),
+    "scl_debug_counters": ([ctypes.POINTER(_U64), ctypes.POINTER(_U64)], _I),
+    "scl_debug_fp32_peak": ([_I, _U32, _VP, _U64, ctypes.POINTER(_U64)], _I),
     "scl_graph_begin": ([], _I), "scl_graph_end": ([ctypes.POINTER(_VP)], _I),
     "scl_graph_launch": ([_VP], _I), "scl_graph_destroy": ([_VP], _I),
     "scl_debug_bounded_wait": ([_U32, ctypes.POINTER(_I)], _I),
@@ -282,6 +285,20 @@ def compile_only(kind: int, source: str, types: Sequence[str], **kw) -> str:
     log = ctypes.create_string_buffer(1 << 16)
     check(lib().scl_program_compile(ctypes.byref(d), log, len(log)))
     return log.value.decode(errors="replace")
+
+
+def debug_counters() -> dict:
+    """Device allocations and module loads the library has made."""
+    a, m = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    check(lib().scl_debug_counters(ctypes.byref(a), ctypes.byref(m)))
+    return {"device_allocs": a.value, "module_loads": m.value}
+
+
+def cache_stats() -> dict:
+    """Counters of the program binary cache since the library was loaded."""
+    v = [ctypes.c_uint64(0) for _ in range(4)]
+    check(lib().scl_cache_stats(*[ctypes.byref(x) for x in v]))
+    return dict(zip(("nvrtc_compiles", "disk_loads", "disk_rejects", "disk_saves"), (x.value for x in v)))
 
 
 def generated_source(kind: int, source: str, types: Sequence[str], **kw) -> str:

@@ -71,6 +71,8 @@ struct Runtime {
   unsigned int* dev_err = nullptr;   // device-side status word
   unsigned int* host_err = nullptr;  // pinned mirror
   uint64_t launches = 0;
+  uint64_t device_allocs = 0;  // device allocations made by the library (scl_alloc included)
+  uint64_t module_loads = 0;   // cubins loaded
   bool capturing = false;
   Driver drv;
 };
@@ -110,7 +112,46 @@ struct Kernel {
 struct Workspace {  // per-program scratch (reduce partials, scan tile status)
   void* ptr = nullptr;
   size_t bytes = 0;
+  // Scan status (scan.cuh): tiles per region, the allocation that layout
+  // was cleared in, launches made since, and the slots the last launch in
+  // each of the two alternating regions may have written
+  uint64_t scan_cap = 0;
+  void* scan_layout = nullptr;
+  uint64_t scan_epoch = 0;
+  uint64_t scan_used[2] = {0, 0};
 };
+
+// Scan status layout (scan.cuh): three regions of `cap` tiles, each a
+// 128-byte ticket line followed by one 128-byte line per tile (modes 1, 2)
+// or [flags | aggregates | inclusive prefixes] (mode 0).  Eager launches
+// alternate between regions 0 and 1, each clearing the other for the next
+// launch; a launch recorded into a graph uses region 2, which the graph
+// clears before the kernel.  Zeroed once per layout.
+size_t scan_region_bytes(int status_mode, size_t carry, uint64_t cap);
+size_t scan_status_bytes(int status_mode, size_t carry, uint64_t cap);
+// Bytes at the start of a region that must be zero before a launch of
+// `tiles` tiles uses it (ticket line and status words / flags).
+size_t scan_region_clear_bytes(int status_mode, uint64_t tiles);
+// Kernel arguments (scan.cuh's scl_scan_status and scl_scan_clear).
+struct ScanStatusArgs {
+  void* slots;
+  void* flags;
+  void* agg;
+  void* incl;
+};
+struct ScanClearArgs {
+  void* slots;
+  void* flags;
+  void* ticket;
+  uint64_t n;
+};
+// Region `r` of a layout at `base`: its ticket word and status pointers.
+ScanStatusArgs scan_region(void* base, int status_mode, size_t carry, uint64_t cap, int r,
+                           void** ticket);
+// Tiles of `tile` elements a scan of n elements at `in` launches (the staged
+// kernel lays them on the 16-byte grid of `in`: scan_grid gives the grid).
+void scan_grid(const void* in, size_t tsz, bool staged, uint64_t* vg, uint64_t* a);
+uint64_t scan_tiles(const void* in, size_t tsz, uint64_t n, uint64_t tile, bool staged, bool reverse);
 
 }  // namespace scl
 

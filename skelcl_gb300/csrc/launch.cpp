@@ -447,6 +447,52 @@ static int launch_zipreduce(scl_program* p, const scl_shape* sh, void* const* bu
 }
 
 // ---- Scan ---------------------------------------------------------------------
+namespace scl {
+size_t scan_region_bytes(int status_mode, size_t carry, uint64_t cap) {
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  if (status_mode != 0) return 256 + up(cap * 128);
+  return 256 + up(cap * 4) + 2 * up(cap * carry);
+}
+size_t scan_status_bytes(int status_mode, size_t carry, uint64_t cap) {
+  return 3 * scan_region_bytes(status_mode, carry, cap);
+}
+size_t scan_region_clear_bytes(int status_mode, uint64_t tiles) {
+  return 256 + (status_mode != 0 ? tiles * 128 : tiles * 4);
+}
+ScanStatusArgs scan_region(void* base, int status_mode, size_t carry, uint64_t cap, int r,
+                           void** ticket) {
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  char* b = static_cast<char*>(base) + (size_t)r * scan_region_bytes(status_mode, carry, cap);
+  if (ticket) *ticket = b;
+  ScanStatusArgs a = {nullptr, nullptr, nullptr, nullptr};
+  if (status_mode != 0) {
+    a.slots = b + 256;
+  } else {
+    a.flags = b + 256;
+    a.agg = b + 256 + up(cap * 4);
+    a.incl = b + 256 + up(cap * 4) + up(cap * carry);
+  }
+  return a;
+}
+// The staged kernel lays tiles on the 16-byte grid of `in`: first element
+// index `a` on a 16-byte boundary, one grid point every `vg` elements (vg = 1
+// and a = 0 without a grid: odd element sizes, misaligned pointers, or the
+// register kernel).
+void scan_grid(const void* in, size_t tsz, bool staged, uint64_t* vg, uint64_t* a) {
+  const bool grid = staged && (tsz == 4 || tsz == 8 || tsz == 16) &&
+                    reinterpret_cast<uintptr_t>(in) % tsz == 0;
+  *vg = grid ? 16 / tsz : 1;
+  *a = grid ? ((16u - (reinterpret_cast<uintptr_t>(in) & 15u)) & 15u) / tsz : 0;
+}
+uint64_t scan_tiles(const void* in, size_t tsz, uint64_t n, uint64_t tile, bool staged, bool reverse) {
+  uint64_t vg, ga;
+  scan_grid(in, tsz, staged, &vg, &ga);
+  if (!staged) return (n + tile - 1) / tile;
+  const uint64_t m = reverse ? (ga + vg - n % vg) % vg : (vg - ga) % vg;
+  return (n + m + tile - 1) / tile;
+}
+}  // namespace scl
+
 static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bufs,
                                const void* extra, size_t extra_bytes, const scl_tuning* tu) {
   if (int st = check_prog(p, {SCL_KIND_SCAN, SCL_KIND_SCAN_MAP})) return st;
@@ -462,12 +508,13 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   int aligned = (aligned16(in) && aligned16(out)) ? 1 : 0;
   // 32 KB tiles by default: fewer tiles to look back over (measured on GB300)
   uint32_t R = (tu && tu->items) ? tu->items : 8;
-  if (R != 2 && R != 4 && R != 8 && R != 16) R = 8;
+  if (R != 2 && R != 4 && R != 6 && R != 8 && R != 16) R = 8;
   // default: the shared-memory staged kernel (measured 5.7 TB/s on int32 2^28
   // against 5.1 for the tile held in registers); SCL_VARIANT_VECTOR selects
   // the register kernel
   bool staged = !(tu && tu->variant == SCL_VARIANT_VECTOR) || p->kind == SCL_KIND_SCAN_MAP;
   if (staged && R == 2) R = 4;
+  if (!staged && R == 6) R = 8;
   size_t smem = staged ? (size_t)R * 256 * V * tsz : 0;
   if (staged && smem + 2048 > rt().smem_optin) {
     if (p->kind == SCL_KIND_SCAN_MAP)
@@ -485,30 +532,23 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
       return fail(SCL_ERR_UNSUPPORTED, "segmented scan: the tile does not fit in shared memory");
   }
   const uint64_t tile = (uint64_t)R * 256 * V;
-  // the staged kernel lays tiles on the 16-byte grid of `in` (first element
-  // index a on a boundary, every vg elements); the same rule counts them here
-  const bool grid = staged && (tsz == 4 || tsz == 8 || tsz == 16) &&
-                    reinterpret_cast<uintptr_t>(in) % tsz == 0;
-  const uint64_t vg = grid ? (uint64_t)V : 1;
-  const uint64_t ga = grid ? ((16u - (reinterpret_cast<uintptr_t>(in) & 15u)) & 15u) / tsz : 0;
+  uint64_t vg = 1, ga = 0;
+  scan_grid(in, tsz, staged, &vg, &ga);
   uint64_t tiles;
   if (n_seg) {
     // an upper bound (the pre-pass has the count): tiles exist only for
     // segments longer than kSegShort, at most n / tile + 2 per such segment
     const uint64_t n_long = std::min<uint64_t>(n_seg, n / (kSegShort + 1) + 1);
     tiles = (n + tile - 1) / tile + 2 * n_long;
-  } else if (staged) {
-    const uint64_t m = reverse ? (ga + vg - n % vg) % vg : (vg - ga) % vg;
-    tiles = (n + m + tile - 1) / tile;
   } else {
-    tiles = (n + tile - 1) / tile;
+    tiles = scan_tiles(in, tsz, n, tile, staged, reverse);
   }
   if (tiles > 0x7fffffffull) return fail(SCL_ERR_ARG, "scan input too large");
   // resident tiles per SM the register (or shared-memory) budget is sized for
   uint32_t minb = (tu && tu->tile_w) ? tu->tile_w : 0;
   if (staged) {
     if (!((R == 16 && (minb == 2 || minb == 3)) || (R == 8 && minb >= 4 && minb <= 6) ||
-          (R == 4 && minb == 8)))
+          (R == 6 && minb == 8) || (R == 4 && minb == 8)))
       minb = R == 16 ? 3 : (R == 8 ? 6 : 8);
   } else if (!((R == 16 && (minb == 1 || minb == 2)) || (R == 8 && (minb == 2 || minb == 3 || minb == 4)) ||
                (R == 4 && (minb == 4 || minb == 6)) || (R == 2 && minb == 8))) {
@@ -519,37 +559,42 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
                             ", " + std::to_string(minb) + (n_seg ? ", 1>" : ">");
   CUfunction fn = find_kernel(p, kname);
   if (!fn) return fail(SCL_ERR_LAUNCH, "kernel " + kname + " missing");
-  // workspace: [tile counter | status words / flags | values], zeroed by one memset
+  // workspace: three status regions (scan_region_bytes); segmented launches
+  // add [clamped offsets | tile numbering | pre-pass scratch] after them
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-  struct StatusArgs {
-    void* slots;
-    void* flags;
-    void* agg;
-    void* incl;
-  } sargs = {nullptr, nullptr, nullptr, nullptr};
-  // segmented launches add [clamped offsets | tile numbering | pre-pass
-  // scratch] after the status
-  size_t clear_bytes, total;
   const size_t seg_of = n_seg ? up((n_seg + 1) * 8) : 0, seg_ts = n_seg ? up((n_seg + 1) * 4) : 0,
                seg_sc = n_seg ? up(segments_prepare_scratch(n_seg)) : 0;
-  if (p->status_mode != 0) {
-    clear_bytes = 256 + up(tiles * 128);  // one 128-byte line per tile slot
-    total = clear_bytes;
-    if (int st = ensure_workspace(p, total + seg_of + seg_ts + seg_sc)) return st;
-    sargs.slots = (char*)p->ws.ptr + 256;
-  } else {
-    const size_t fl = up(tiles * 4), vals = up(tiles * csz);
-    clear_bytes = 256 + fl;
-    total = clear_bytes + 2 * vals;
-    if (int st = ensure_workspace(p, total + seg_of + seg_ts + seg_sc)) return st;
-    sargs.flags = (char*)p->ws.ptr + 256;
-    sargs.agg = (char*)p->ws.ptr + 256 + fl;
-    sargs.incl = (char*)p->ws.ptr + 256 + fl + vals;
+  Workspace& ws = p->ws;
+  const uint64_t cap = std::max<uint64_t>({tiles, ws.scan_cap, 256});
+  const size_t total = scan_status_bytes(p->status_mode, csz, cap);
+  if (int st = ensure_workspace(p, total + seg_of + seg_ts + seg_sc)) return st;
+  if (cap != ws.scan_cap || ws.scan_layout != ws.ptr) {
+    SCL_CUDA(cudaMemsetAsync(ws.ptr, 0, total, rt().stream));
+    ws.scan_cap = cap;
+    ws.scan_layout = ws.ptr;
+    ws.scan_epoch = 0;
+    ws.scan_used[0] = ws.scan_used[1] = 0;
   }
-  void* counter = p->ws.ptr;
-  void* seg_off = n_seg ? (char*)p->ws.ptr + total : nullptr;
-  void* tile_start = n_seg ? (char*)p->ws.ptr + total + seg_of : nullptr;
-  SCL_CUDA(cudaMemsetAsync(p->ws.ptr, 0, clear_bytes, rt().stream));
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  SCL_CUDA(cudaStreamIsCapturing(rt().stream, &capture));
+  const bool recorded = capture != cudaStreamCaptureStatusNone;
+  // eager launches alternate between regions 0 and 1 and clear the other
+  // one for the next launch; a recorded launch uses region 2 and the graph
+  // clears it first, so every replay finds it clean
+  const int region = recorded ? 2 : (int)(ws.scan_epoch & 1);
+  void* counter = nullptr;
+  ScanStatusArgs sargs = scan_region(ws.ptr, p->status_mode, csz, cap, region, &counter);
+  ScanClearArgs clr = {nullptr, nullptr, nullptr, 0};
+  if (recorded) {
+    SCL_CUDA(cudaMemsetAsync(counter, 0, scan_region_clear_bytes(p->status_mode, tiles), rt().stream));
+  } else {
+    ScanStatusArgs o = scan_region(ws.ptr, p->status_mode, csz, cap, region ^ 1, &clr.ticket);
+    clr.slots = o.slots;
+    clr.flags = o.flags;
+    clr.n = ws.scan_used[region ^ 1];
+  }
+  void* seg_off = n_seg ? (char*)ws.ptr + total : nullptr;
+  void* tile_start = n_seg ? (char*)ws.ptr + total + seg_of : nullptr;
   if (n_seg) {
     uint64_t short_max = kSegShort;
     uint64_t* scratch = reinterpret_cast<uint64_t*>((char*)p->ws.ptr + total + seg_of + seg_ts);
@@ -572,7 +617,7 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   unsigned int spin = spin_of(tu);
   unsigned int* err = rt().dev_err;
   ArgPack pack;
-  pack.ptrs = {&in, &out, &n, &flags, &aligned, &counter, &sargs, &spin, &err};
+  pack.ptrs = {&in, &out, &n, &flags, &aligned, &counter, &sargs, &clr, &spin, &err};
   if (staged) {
     pack.ptrs.push_back(&seg_off);
     pack.ptrs.push_back(&tile_start);
@@ -581,7 +626,13 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
     return st;
   p->last_variant = staged ? SCL_VARIANT_TMA : SCL_VARIANT_VECTOR;
-  return launch(fn, dim3((unsigned)tiles), dim3(256), smem, pack);
+  if (int st = launch(fn, dim3((unsigned)tiles), dim3(256), smem, pack)) return st;
+  if (!recorded) {  // this launch's region now holds up to `tiles` slots; the other is clean
+    ws.scan_used[region] = tiles;
+    ws.scan_used[region ^ 1] = 0;
+    ws.scan_epoch++;
+  }
+  return SCL_OK;
 }
 
 // ---- MapOverlap -----------------------------------------------------------------

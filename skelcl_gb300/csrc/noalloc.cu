@@ -24,10 +24,12 @@ void* g_noalloc_addr[kMaxDevices] = {};
 
 size_t round256(size_t b) { return (b + 255) / 256 * 256; }
 
-// Scratch bytes for `tiles` tiles, the layout scl_launch_scan uses:
-// [counter | status] where status is one 128-byte line per tile (carries of
-// at most 4 bytes, or double) or [flags | aggregates | inclusive prefixes].
-// `clear` receives the bytes that must start at zero.
+// Scratch bytes for `tiles` tiles in the layout of scl_launch_scan (one
+// status half: every call starts from a cleared array, so the kernel only
+// ever uses half 0): [control words | status], the status being one 128-byte
+// line per tile (carries of at most 4 bytes, or double) or [flags |
+// aggregates | inclusive prefixes].  `clear` receives the bytes that must
+// start at zero.
 size_t scratch_bytes(int status_mode, size_t carry, uint64_t tiles, size_t* clear) {
   if (status_mode != 0) {
     *clear = kCounterBytes + round256(tiles * 128);
@@ -72,13 +74,22 @@ extern "C" int scl_launch_scan_noalloc(scl_program* p, const scl_shape* sh, void
   if (p->kind != SCL_KIND_SCAN)
     return fail(SCL_ERR_ARG, "scl_launch_scan_noalloc needs a Scan program");
   if (!sh || !bufs || !bufs[0] || !bufs[1]) return fail(SCL_ERR_ARG, "scan needs {in, out}");
+  if (sh->n_segments)
+    return fail(SCL_ERR_UNSUPPORTED,
+                "scl_launch_scan_noalloc scans one vector; segmented scans need scl_launch_scan");
   void* in = bufs[0];
   void* out = bufs[1];
   uint64_t n = sh->n;
+  const unsigned int flags = sh->flags & (SCL_SHAPE_INCLUSIVE | SCL_SHAPE_REVERSE);
+  const bool reverse = (flags & SCL_SHAPE_REVERSE) != 0;
   const size_t tsz = p->type_sizes[0], csz = p->carry_size ? p->carry_size : tsz;
   const uint64_t V = (tsz <= 16 && 16 % tsz == 0) ? 16 / tsz : 1;  // as the kernel's scl_vec_width
-  const uint64_t tile = 8 * 256 * V;                                 // default shape: 8 rows x 256 threads
-  const uint64_t tiles = n / tile + (n % tile != 0 ? 1 : 0);
+  const uint64_t tile = 8 * 256 * V;                                 // 8 rows x 256 threads
+  // scl_launch_scan's default kernel (the tile staged in shared memory), or
+  // the register kernel when the tile does not fit in shared memory
+  const size_t smem = (size_t)tile * tsz;
+  const bool staged = smem + 2048 <= rt().smem_optin;
+  const uint64_t tiles = scan_tiles(in, tsz, n, tile, staged, reverse);
 
   // size check before anything touches the GPU
   const uint64_t cap = SCL_NOALLOC_SCRATCH_BYTES;
@@ -91,29 +102,32 @@ extern "C" int scl_launch_scan_noalloc(scl_program* p, const scl_shape* sh, void
       size_t c;
       if (scratch_bytes(p->status_mode, csz, mid, &c) <= cap) lo = mid; else hi = mid - 1;
     }
+    // an input that does not start on a 16-byte boundary may need one tile
+    // more (the staged kernel lays tiles on the 16-byte grid)
     return fail(SCL_ERR_ARG, "scl_launch_scan_noalloc: " + std::to_string(n) + " elements of " +
                                  std::to_string(tsz) + " bytes need more than the fixed " +
                                  std::to_string(cap) + "-byte scratch; it holds at most " +
                                  std::to_string(lo * tile) +
-                                 " elements of this type (scl_launch_scan has no such limit)");
+                                 " elements of this type starting on a 16-byte boundary (" +
+                                 std::to_string(lo > 0 ? (lo - 1) * tile : 0) +
+                                 " otherwise; scl_launch_scan has no such limit)");
   }
   if (n == 0) return SCL_OK;
   if (tiles > 0x7fffffffull) return fail(SCL_ERR_ARG, "scan input too large");
 
-  // only the kernel loaded when the program was built: no module load here
-  auto it = p->kernels.find("scl_scan_k<8, 4>");
+  // only kernels loaded when the program was built: no module load here
+  const char* kname = staged ? "scl_scan_s<8, 6>" : "scl_scan_k<8, 4>";
+  auto it = p->kernels.find(kname);
   if (it == p->kernels.end() || !it->second.fn)
-    return fail(SCL_ERR_LAUNCH, "kernel scl_scan_k<8, 4> missing from the program");
+    return fail(SCL_ERR_LAUNCH, std::string("kernel ") + kname + " missing from the program");
   CUfunction fn = it->second.fn;
 
   void* base = nullptr;
   if (int st = scratch_address(rt().device, &base)) return st;
-  struct StatusArgs {
-    void* slots;
-    void* flags;
-    void* agg;
-    void* incl;
-  } sargs = {nullptr, nullptr, nullptr, nullptr};
+  // one status region of `tiles` tiles after the ticket line, cleared by
+  // every call (nothing for the kernel to clear for a next launch)
+  ScanStatusArgs sargs = {nullptr, nullptr, nullptr, nullptr};
+  ScanClearArgs clr = {nullptr, nullptr, nullptr, 0};
   char* b = static_cast<char*>(base);
   if (p->status_mode != 0) {
     sargs.slots = b + kCounterBytes;
@@ -123,18 +137,26 @@ extern "C" int scl_launch_scan_noalloc(scl_program* p, const scl_shape* sh, void
     sargs.agg = b + kCounterBytes + fl;
     sargs.incl = b + kCounterBytes + fl + vals;
   }
-  void* counter = base;
-  // the previous call left its counter and status behind
+  void* ticket = base;
+  // the previous call left its ticket and status behind
   SCL_CUDA(cudaMemsetAsync(base, 0, clear, rt().stream));
 
-  unsigned int flags = sh->flags & (SCL_SHAPE_INCLUSIVE | SCL_SHAPE_REVERSE);
+  unsigned int fl = flags;
   int aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0;
   unsigned int spin = (tu && tu->spin_limit) ? tu->spin_limit : (1u << 22);
   unsigned int* err = rt().dev_err;
+  const void* seg_off = nullptr;
+  const void* tile_start = nullptr;
+  uint64_t n_seg = 0;
   ArgPack pack;
-  pack.ptrs = {&in, &out, &n, &flags, &aligned, &counter, &sargs, &spin, &err};
+  pack.ptrs = {&in, &out, &n, &fl, &aligned, &ticket, &sargs, &clr, &spin, &err};
+  if (staged) {
+    pack.ptrs.push_back(&seg_off);
+    pack.ptrs.push_back(&tile_start);
+    pack.ptrs.push_back(&n_seg);
+  }
   if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
     return st;
-  p->last_variant = SCL_VARIANT_VECTOR;
-  return launch(fn, dim3((unsigned)tiles), dim3(256), 0, pack);
+  p->last_variant = staged ? SCL_VARIANT_TMA : SCL_VARIANT_VECTOR;
+  return launch(fn, dim3((unsigned)tiles), dim3(256), staged ? smem : 0, pack);
 }

@@ -23,12 +23,14 @@
 // SKELCL_COMPILE_ALL=YES compiles every kernel variant at construction.
 #include <nvrtc.h>
 
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <sstream>
 #include <sys/stat.h>
+#include <unistd.h>
 
 #include "internal.h"
 
@@ -347,7 +349,7 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
       out->kernels = {"scl_scan_s<8, 6>", "scl_scan_k<8, 4>"};
       out->lazy = {"scl_scan_k<8, 3>", "scl_scan_k<8, 2>", "scl_scan_k<4, 4>", "scl_scan_k<4, 6>",
                    "scl_scan_k<2, 8>", "scl_scan_k<16, 2>", "scl_scan_k<16, 1>",
-                   "scl_scan_s<8, 5>", "scl_scan_s<8, 4>", "scl_scan_s<4, 8>",
+                   "scl_scan_s<8, 5>", "scl_scan_s<8, 4>", "scl_scan_s<4, 8>", "scl_scan_s<6, 8>",
                    "scl_scan_s<16, 3>", "scl_scan_s<8, 6, 1>", "scl_scan_s<16, 3, 1>",
                    "scl_scan_short<8>"};
       break;
@@ -358,7 +360,8 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
     case SCL_KIND_SCAN_MAP:
       s << scl_tpl_reduce << "\n" << scl_tpl_scan;
       out->kernels = {"scl_scan_s<8, 6>"};
-      out->lazy = {"scl_scan_s<8, 5>", "scl_scan_s<8, 4>", "scl_scan_s<4, 8>", "scl_scan_s<16, 3>",
+      out->lazy = {"scl_scan_s<8, 5>", "scl_scan_s<8, 4>", "scl_scan_s<4, 8>", "scl_scan_s<6, 8>",
+                   "scl_scan_s<16, 3>",
                    "scl_scan_s<8, 6, 1>", "scl_scan_s<16, 3, 1>", "scl_scan_short<8>"};
       break;
     case SCL_KIND_MAPOVERLAP:
@@ -412,27 +415,56 @@ std::string cache_dir() {
   return (home.empty() ? std::string("/tmp") : home) + "/.cache/skelcl_gb300";
 }
 
-// Serialised cache entry: "SCLBIN1\n" n_names \n (expr \n lowered \n)* cubin
+// Counters of the compile cache (scl_cache_stats).
+std::atomic<uint64_t> g_nvrtc_compiles{0}, g_disk_loads{0}, g_disk_rejects{0}, g_disk_saves{0};
+
+std::string cache_file(const std::string& key) { return cache_dir() + "/" + key + ".sm_103a.skelcl"; }
+
+// Serialised cache entry (text header, then the cubin):
+//   SCLBIN2 \n key \n n_names \n (name \n lowered name \n)* cubin_bytes sha1(cubin) \n cubin
+// A file that is not exactly this -- another format or key, a name list
+// that does not parse, fewer or more cubin bytes than recorded, a cubin whose
+// SHA-1 differs or that is not an ELF image -- is rejected and the program is
+// compiled instead (SKELCL_SAVE_BINARY then replaces the file).
 bool load_disk(const std::string& key, std::string* cubin,
                std::map<std::string, std::string>* names) {
-  std::ifstream f(cache_dir() + "/" + key + ".sm_103a.skelcl", std::ios::binary);
-  if (!f) return false;
-  std::string magic;
-  std::getline(f, magic);
-  if (magic != "SCLBIN1") return false;
-  std::string line;
-  std::getline(f, line);
-  int n = std::atoi(line.c_str());
-  for (int i = 0; i < n; ++i) {
+  std::ifstream f(cache_file(key), std::ios::binary);
+  if (!f) return false;  // no entry: not a reject
+  auto reject = [&]() {
+    g_disk_rejects++;
+    names->clear();
+    cubin->clear();
+    return false;
+  };
+  std::string magic, k, line;
+  if (!std::getline(f, magic) || magic != "SCLBIN2") return reject();
+  if (!std::getline(f, k) || k != key) return reject();
+  if (!std::getline(f, line)) return reject();
+  char* end = nullptr;
+  const long n = std::strtol(line.c_str(), &end, 10);
+  if (end == line.c_str() || *end != '\0' || n < 1 || n > 4096) return reject();
+  std::map<std::string, std::string> got;
+  for (long i = 0; i < n; ++i) {
     std::string a, b;
-    std::getline(f, a);
-    std::getline(f, b);
-    (*names)[a] = b;
+    if (!std::getline(f, a) || !std::getline(f, b) || a.empty() || b.empty()) return reject();
+    got[a] = b;
   }
-  std::ostringstream rest;
-  rest << f.rdbuf();
-  *cubin = rest.str();
-  return !cubin->empty();
+  if (!std::getline(f, line)) return reject();
+  const size_t sp = line.find(' ');
+  if (sp == std::string::npos) return reject();
+  const unsigned long long bytes = std::strtoull(line.substr(0, sp).c_str(), &end, 10);
+  const std::string digest = line.substr(sp + 1);
+  if (bytes < 4 || bytes > (1ull << 31)) return reject();
+  std::string bin((size_t)bytes, '\0');
+  f.read(&bin[0], (std::streamsize)bytes);
+  if ((unsigned long long)f.gcount() != bytes) return reject();  // truncated
+  if (f.peek() != std::char_traits<char>::eof()) return reject();  // trailing bytes
+  if (bin.compare(0, 4, "\x7f" "ELF") != 0) return reject();
+  if (sha1_hex(bin.data(), bin.size()) != digest) return reject();
+  *cubin = std::move(bin);
+  *names = std::move(got);
+  g_disk_loads++;
+  return true;
 }
 
 void save_disk(const std::string& key, const std::string& cubin,
@@ -445,15 +477,22 @@ void save_disk(const std::string& key, const std::string& cubin,
     }
     if (i < dir.size()) acc += dir[i];
   }
-  std::string tmp = dir + "/" + key + ".tmp";
+  std::string tmp = dir + "/" + key + ".tmp" + std::to_string((unsigned long)getpid());
   {
     std::ofstream f(tmp, std::ios::binary);
     if (!f) return;
-    f << "SCLBIN1\n" << names.size() << "\n";
+    f << "SCLBIN2\n" << key << "\n" << names.size() << "\n";
     for (auto& kv : names) f << kv.first << "\n" << kv.second << "\n";
+    f << cubin.size() << " " << sha1_hex(cubin.data(), cubin.size()) << "\n";
     f.write(cubin.data(), (std::streamsize)cubin.size());
+    if (!f) {
+      f.close();
+      std::remove(tmp.c_str());
+      return;
+    }
   }
-  std::rename(tmp.c_str(), (dir + "/" + key + ".sm_103a.skelcl").c_str());
+  if (std::rename(tmp.c_str(), cache_file(key).c_str()) == 0) g_disk_saves++;
+  else std::remove(tmp.c_str());
 }
 
 int nvrtc_compile(const Assembly& a, std::string* cubin,
@@ -467,6 +506,7 @@ int nvrtc_compile(const Assembly& a, std::string* cubin,
   for (auto& k : a.kernels)
     if (k.find('<') != std::string::npos) nvrtcAddNameExpression(prog, k.c_str());
   r = nvrtcCompileProgram(prog, kNvrtcOptCount, kNvrtcOpts);
+  g_nvrtc_compiles++;
   size_t ls = 0;
   nvrtcGetProgramLogSize(prog, &ls);
   std::string lg(ls, '\0');
@@ -500,13 +540,35 @@ void copy_log(const std::string& s, char* log, size_t cap) {
   log[n] = '\0';
 }
 
+// Everything a cached cubin depends on besides the source and the kernel
+// names: the NVRTC options (target sm_103a), NVRTC's version, the ABI
+// version of this library and, once a device is open, its compute
+// capability and driver version.  The reference names its binaries by
+// source hash and device (src/Program.cpp:62-75).
+std::string cache_context() {
+  std::string k;
+  for (int i = 0; i < kNvrtcOptCount; ++i) k += std::string("\n") + kNvrtcOpts[i];
+  int major = 0, minor = 0;
+  nvrtcVersion(&major, &minor);
+  k += "\n#nvrtc " + std::to_string(major) + "." + std::to_string(minor);
+  k += "\n#abi " + std::to_string(SCL_ABI_VERSION);
+  if (rt().initialized) {
+    int drv = 0;
+    cudaDriverGetVersion(&drv);
+    k += "\n#device cc" + std::to_string(rt().cc_major) + "." + std::to_string(rt().cc_minor) +
+         " driver " + std::to_string(drv);
+  } else {
+    k += "\n#device none";
+  }
+  return k;
+}
+
 // Compile `names` out of `source` (or take them from the in-process / on-disk
-// cache).  The cache key covers the source, the options and the names.
+// cache).  The cache key covers the source, the names and cache_context().
 int compile_cached(const std::string& source, const std::vector<std::string>& names,
                    std::string* cubin, std::map<std::string, std::string>* lowered,
                    std::string* nvlog, std::string* hash) {
-  std::string k = source;
-  for (int i = 0; i < kNvrtcOptCount; ++i) k += std::string("\n") + kNvrtcOpts[i];
+  std::string k = source + cache_context();
   for (auto& n : names) k += "\n#name " + n;
   const std::string key = sha1_hex(k.data(), k.size());
   if (hash) *hash = sha1_hex(source.data(), source.size());
@@ -543,6 +605,7 @@ int load_module(scl_program* p, const std::string& cubin,
   Driver& drv = rt().drv;
   CUmodule mod = nullptr;
   CUresult r = drv.cuModuleLoadData(&mod, cubin.data());
+  rt().module_loads++;
   if (r != CUDA_SUCCESS) return cu_fail(r, "cuModuleLoadData");
   p->modules.push_back(mod);
   for (auto& kv : lowered) {
@@ -582,6 +645,7 @@ int ensure_workspace(scl_program* p, size_t bytes) {
   }
   size_t sz = bytes < 4096 ? 4096 : bytes;
   cudaError_t e = cudaMalloc(&p->ws.ptr, sz);
+  rt().device_allocs++;
   if (e != cudaSuccess) return fail(SCL_ERR_OOM, "workspace allocation of " + std::to_string(sz) + " bytes failed");
   // zeroed once: reduce tickets rely on it and reset themselves afterwards
   e = cudaMemset(p->ws.ptr, 0, sz);
@@ -594,10 +658,65 @@ int ensure_workspace(scl_program* p, size_t bytes) {
 
 using namespace scl;
 
+namespace {
+// Builds the program's source and compiles its kernels (every variant when
+// `all`, else the eager ones): with FP64 carries when the element type asks
+// for them and the eager kernels compile that way, else with carries in the
+// element type.  The eager kernels alone decide the carry type, so a lazy
+// variant that fails to compile is reported as the error it is instead of
+// silently changing the carries of the default kernels.
+int compile_program(const scl_program_desc* desc, scl_program* p, bool all, Assembly* a,
+                    std::string* cubin, std::map<std::string, std::string>* lowered,
+                    std::string* nvlog, std::string* err, bool* f64_used, std::string* hash) {
+  const bool want_f64 = wants_f64_carry(desc);
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    const bool f64 = want_f64 && attempt == 0;
+    *a = Assembly();
+    int st = assemble(desc, p, f64, a, err);
+    if (st != SCL_OK) return st;
+    const std::vector<std::string> eager = a->kernels;
+    if (all) {
+      a->kernels.insert(a->kernels.end(), a->lazy.begin(), a->lazy.end());
+      a->lazy.clear();
+    }
+    lowered->clear();
+    st = compile_cached(a->source, a->kernels, cubin, lowered, nvlog, hash);
+    if (st == SCL_OK) {
+      *f64_used = f64;
+      return SCL_OK;
+    }
+    if (f64 && all) {
+      std::string c2, l2;
+      std::map<std::string, std::string> w2;
+      if (compile_cached(a->source, eager, &c2, &w2, &l2, nullptr) == SCL_OK) {
+        *err = "NVRTC compilation of a kernel variant failed:\n" + *nvlog;
+        return SCL_ERR_COMPILE;
+      }
+    }
+    if (!f64) break;
+  }
+  *err = "NVRTC compilation failed:\n" + *nvlog;
+  return SCL_ERR_COMPILE;
+}
+
+bool compile_all_requested(const scl_program_desc* desc) {
+  return (desc->flags & SCL_PROG_COMPILE_ALL) || env_yes("SKELCL_COMPILE_ALL");
+}
+}  // namespace
+
 extern "C" int scl_sha1_hex(const void* data, size_t bytes, char* out41) {
   if (!out41 || (!data && bytes)) return fail(SCL_ERR_ARG, "scl_sha1_hex: null pointer");
   std::string h = sha1_hex(data, bytes);
   std::memcpy(out41, h.c_str(), 41);
+  return SCL_OK;
+}
+
+extern "C" int scl_cache_stats(uint64_t* nvrtc_compiles, uint64_t* disk_loads,
+                               uint64_t* disk_rejects, uint64_t* disk_saves) {
+  if (nvrtc_compiles) *nvrtc_compiles = g_nvrtc_compiles.load();
+  if (disk_loads) *disk_loads = g_disk_loads.load();
+  if (disk_rejects) *disk_rejects = g_disk_rejects.load();
+  if (disk_saves) *disk_saves = g_disk_saves.load();
   return SCL_OK;
 }
 
@@ -635,32 +754,17 @@ extern "C" int scl_program_build(const scl_program_desc* desc, scl_program** out
   p->padding = desc->padding;
   for (int i = 0; i < desc->n_types; ++i) p->type_names.push_back(desc->type_names[i]);
 
-  bool want_f64 = wants_f64_carry(desc);
   std::string cubin, nvlog, err;
   std::map<std::string, std::string> lowered;
   Assembly a;
-  for (int attempt = 0; attempt < 2; ++attempt) {
-    bool f64 = want_f64 && attempt == 0;
-    int st = assemble(desc, p.get(), f64, &a, &err);
-    if (st != SCL_OK) {
-      copy_log(err, log, log_cap);
-      return fail(st, err);
-    }
-    // every variant now, none on first use (flag, or SKELCL_COMPILE_ALL=YES)
-    if ((desc->flags & SCL_PROG_COMPILE_ALL) || env_yes("SKELCL_COMPILE_ALL")) {
-      a.kernels.insert(a.kernels.end(), a.lazy.begin(), a.lazy.end());
-      a.lazy.clear();
-    }
-    st = compile_cached(a.source, a.kernels, &cubin, &lowered, &nvlog, &p->hash);
-    if (st != SCL_OK) {
-      if (f64) continue;  // retry with carries in the element type
-      std::string msg = "NVRTC compilation failed:\n" + nvlog;
-      copy_log(msg, log, log_cap);
-      return fail(SCL_ERR_COMPILE, msg);
-    }
-    p->f64_carry = f64;
-    break;
+  bool f64 = false;
+  // every variant now, none on first use (flag, or SKELCL_COMPILE_ALL=YES)
+  if (int st = compile_program(desc, p.get(), compile_all_requested(desc), &a, &cubin, &lowered,
+                               &nvlog, &err, &f64, &p->hash)) {
+    copy_log(err, log, log_cap);
+    return fail(st, err);
   }
+  p->f64_carry = f64;
   p->source = a.source;
   for (auto& k : a.lazy) p->lazy.insert(k);
   if (int st = require_init()) {
@@ -692,28 +796,17 @@ extern "C" int scl_program_compile(const scl_program_desc* desc, char* log, size
   if (!desc) return fail(SCL_ERR_ARG, "scl_program_compile: null desc");
   scl_program tmp;
   tmp.kind = desc->kind;
-  bool want_f64 = wants_f64_carry(desc);
   std::string err, nvlog, cubin;
   std::map<std::string, std::string> lowered;
-  for (int attempt = 0; attempt < 2; ++attempt) {
-    Assembly a;
-    bool f64 = want_f64 && attempt == 0;
-    int st = assemble(desc, &tmp, f64, &a, &err);
-    if (st != SCL_OK) {
-      copy_log(err, log, log_cap);
-      return fail(st, err);
-    }
-    if (desc->flags & SCL_PROG_COMPILE_ALL) a.kernels.insert(a.kernels.end(), a.lazy.begin(), a.lazy.end());
-    st = nvrtc_compile(a, &cubin, &lowered, &nvlog);
-    if (st == SCL_OK) {
-      copy_log(nvlog, log, log_cap);
-      return SCL_OK;
-    }
-    if (!f64) break;
+  Assembly a;
+  bool f64 = false;
+  if (int st = compile_program(desc, &tmp, compile_all_requested(desc), &a, &cubin, &lowered, &nvlog,
+                               &err, &f64, nullptr)) {
+    copy_log(err, log, log_cap);
+    return fail(st, err);
   }
-  std::string msg = "NVRTC compilation failed:\n" + nvlog;
-  copy_log(msg, log, log_cap);
-  return fail(SCL_ERR_COMPILE, msg);
+  copy_log(nvlog, log, log_cap);
+  return SCL_OK;
 }
 
 extern "C" int scl_program_release(scl_program* p) {

@@ -75,6 +75,49 @@ __global__ void scl_bounded_wait_kernel(const unsigned int* flag, unsigned int p
   }
   *status = SCL_OK;
 }
+
+// FP32 peak probe: 16 independent FMA chains per thread (scalar fma.rn.f32,
+// or packed fma.rn.f32x2 on 8 pairs), `iters` rounds, no memory traffic
+// but one float per thread at the end.  m and c arrive as arguments so the
+// chains cannot be folded.
+template <int PACKED>
+__global__ void __launch_bounds__(256) scl_fma_peak_kernel(float* sink, unsigned int iters, float m,
+                                                           float c) {
+  const float base = (float)(threadIdx.x & 31) * 1e-3f;
+  float r = 0.0f;
+  if constexpr (PACKED) {
+    unsigned long long a[8], mm, cc;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(mm) : "f"(m));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(cc) : "f"(c));
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const float lo = base + (float)(2 * k), hi = base + (float)(2 * k + 1);
+      asm("mov.b64 %0, {%1, %2};" : "=l"(a[k]) : "f"(lo), "f"(hi));
+    }
+    for (unsigned int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        asm volatile("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(a[k]) : "l"(mm), "l"(cc));
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      float lo, hi;
+      asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a[k]));
+      r += lo + hi;
+    }
+  } else {
+    float a[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) a[k] = base + (float)k;
+    for (unsigned int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) a[k] = fmaf(a[k], m, c);
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) r += a[k];
+  }
+  sink[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = r;
+}
 }  // namespace
 
 }  // namespace scl
@@ -175,6 +218,7 @@ extern "C" int scl_alloc(size_t bytes, void** dptr) {
   *dptr = nullptr;
   if (bytes == 0) bytes = 16;
   cudaError_t e = cudaMallocAsync(dptr, bytes, g_rt.stream);
+  g_rt.device_allocs++;
   if (e != cudaSuccess) {
     cudaGetLastError();
     return fail(SCL_ERR_OOM, "scl_alloc: cannot allocate " + std::to_string(bytes) + " bytes (" +
@@ -389,10 +433,32 @@ extern "C" int scl_launch_count(uint64_t* count) {
   return SCL_OK;
 }
 
+extern "C" int scl_debug_counters(uint64_t* device_allocs, uint64_t* module_loads) {
+  if (device_allocs) *device_allocs = g_rt.device_allocs;
+  if (module_loads) *module_loads = g_rt.module_loads;
+  return SCL_OK;
+}
+
+extern "C" int scl_debug_fp32_peak(int packed, uint32_t iters, float* sink, uint64_t sink_floats,
+                                   uint64_t* flops) {
+  if (int st = require_init()) return st;
+  const unsigned int blocks = (unsigned int)g_rt.sm_count * 8u;  // 2048 threads per SM
+  const uint64_t threads = (uint64_t)blocks * 256u;
+  if (!sink || sink_floats < threads)
+    return fail(SCL_ERR_ARG, "scl_debug_fp32_peak: the sink needs " + std::to_string(threads) + " floats");
+  if (packed) scl_fma_peak_kernel<1><<<blocks, 256, 0, g_rt.stream>>>(sink, iters, 0.9999f, 1e-4f);
+  else scl_fma_peak_kernel<0><<<blocks, 256, 0, g_rt.stream>>>(sink, iters, 0.9999f, 1e-4f);
+  SCL_CUDA(cudaGetLastError());
+  ++g_rt.launches;
+  if (flops) *flops = threads * (uint64_t)iters * 16u * 2u;
+  return SCL_OK;
+}
+
 extern "C" int scl_debug_bounded_wait(uint32_t polls, int* status) {
   if (int st = require_init()) return st;
   if (!status) return fail(SCL_ERR_ARG, "null argument");
   unsigned int* buf = nullptr;
+  g_rt.device_allocs++;
   SCL_CUDA(cudaMalloc(&buf, 2 * sizeof(unsigned int)));
   SCL_CUDA(cudaMemset(buf, 0, 2 * sizeof(unsigned int)));
   unsigned int init = 0xffffffffu;

@@ -62,6 +62,13 @@ template <typename C> struct scl_status_mode {
   static constexpr int value = sizeof(C) <= 4 ? 1 : (scl_same<C, double>::value ? 2 : 0);
 };
 
+// Staged kernel: when carries are wider than the elements (FP64 carries of a
+// float scan), each thread folds its lane prefix into the staged tile before
+// the look-back instead of keeping R warp prefixes in registers across it
+// (measured on GB300, f32 2^26: 40 registers with spills -> 29 without, 4.5 %
+// faster; for 4-byte carries keeping them is 1 % faster).
+constexpr bool kLocalPrefix = !scl_same<scl_C, scl_T>::value;
+
 __device__ __forceinline__ unsigned long long scl_ld_relaxed64(const unsigned long long* p) {
   unsigned long long v;
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -116,6 +123,32 @@ struct scl_scan_status {
   scl_C* incl;                // mode 0
 };
 
+// What a launch clears for the next one: the slots (or flags) [0, n) of the
+// status region the previous launch used, and that region's ticket word.
+// The host alternates launches between two regions, so no launch needs a
+// separate clear before it (a launch recorded in a graph uses a third
+// region that the graph clears itself).
+struct scl_scan_clear {
+  unsigned long long* slots;  // modes 1, 2
+  unsigned int* flags;        // mode 0
+  unsigned int* ticket;       // reset to 0 (block 0), or null
+  unsigned long long n;
+};
+
+__device__ __forceinline__ void scl_scan_clear_other(const scl_scan_clear& c) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && c.ticket) *c.ticket = 0u;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < c.n;
+       i += stride) {
+    if constexpr (scl_status_mode<scl_C>::value != 0) {
+      asm volatile("st.global.v2.u64 [%0], {%1, %1};" :: "l"(c.slots + i * SCL_SLOT_STRIDE), "l"(0ull)
+                   : "memory");
+    } else {
+      c.flags[i] = 0u;
+    }
+  }
+}
+
 __device__ __forceinline__ void scl_publish(const scl_scan_status& st, unsigned int tile,
                                             bool inclusive, const scl_C& v) {
   if constexpr (scl_status_mode<scl_C>::value != 0) {
@@ -149,11 +182,59 @@ __device__ __forceinline__ int scl_poll(const scl_scan_status& st, long long idx
   }
 }
 
+// Decoupled look-back of warp 0 (all 32 lanes) for the tile with ticket
+// `tile`, whose sequence starts at ticket `first`: returns the fold of every
+// earlier tile of the sequence, combined as f(earlier, later).  Each round
+// reads 32 predecessors (one per lane, lane l = tile - 1 - l); a round that
+// finds an inclusive prefix ends the look-back, otherwise its aggregates are
+// folded in and the next 32 are read.  (Measured on GB300 and not kept:
+// 64 or 128 predecessors per round, several loads in flight per lane, in
+// every round or only after a first round without an inclusive prefix --
+// all slower, 3-18 %.)
+__device__ __forceinline__ scl_C scl_lookback(const scl_scan_status& st, long long tile, long long first,
+                                              unsigned int spin_limit, unsigned int* err
+                                                  SCL_USER_PARAMS) {
+  const int lane = threadIdx.x & 31;
+  const scl_C cid = (scl_C)(scl_T)(SCL_IDENTITY);
+  scl_C running = cid;  // fold of the tiles already visited (later ones)
+  long long pred = tile - 1;
+  while (true) {
+    const long long idx = pred - lane;
+    scl_C v = cid;
+    int kind = 2;  // before the sequence's first tile: nothing to add, stop here
+    if (idx >= first) {
+      kind = scl_poll(st, idx, spin_limit, &v);
+      if (kind == 0) {
+        scl_raise(err, SCL_DEV_ERR_TIMEOUT);
+        v = cid;
+        kind = 2;
+      }
+    }
+    const unsigned int pmask = __ballot_sync(0xffffffffu, kind == 2);
+    // the usual case: the nearest predecessor already holds its inclusive
+    // prefix, and nothing needs folding (the fold below costs five shuffle
+    // rounds, in FP64 for float carries)
+    if (pmask & 1u) return (scl_C)SCL_FUNC_C(scl_shfl_idx(v, 0), running SCL_OP_ARGS);
+    const int first_inc = pmask ? __ffs(pmask) - 1 : 31;  // nearest inclusive prefix
+    if (lane > first_inc) v = cid;
+    // ordered fold over lanes: higher lane = earlier tile
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      scl_C o = scl_shfl_down(v, off);
+      if (lane + off < 32) v = (scl_C)SCL_FUNC_C(o, v SCL_OP_ARGS);
+    }
+    const scl_C window = scl_shfl_idx(v, 0);
+    running = (scl_C)SCL_FUNC_C(window, running SCL_OP_ARGS);
+    if (pmask) return running;
+    pred -= 32;
+  }
+}
+
 template <int R, int MINB>
 __global__ void __launch_bounds__(SCL_SCAN_B, MINB)  // MINB resident tiles per SM at least
 scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int aligned,
-           unsigned int* tile_counter, scl_scan_status st, unsigned int spin_limit,
-           unsigned int* err SCL_EXTRA_PARAMS) {
+           unsigned int* tile_counter, scl_scan_status st, scl_scan_clear clr,
+           unsigned int spin_limit, unsigned int* err SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
   constexpr int B = SCL_SCAN_B, W = SCL_SCAN_W;
   constexpr int V = scl_vec_width<sizeof(scl_T)>::value;
@@ -164,8 +245,9 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
 
   __shared__ unsigned int s_tile;
   __shared__ scl_T s_wsum[R * W];
-  __shared__ scl_C s_prefix;
+  __shared__ scl_T s_carry;  // the tile's prefix, converted once to the element type
   if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
+  scl_scan_clear_other(clr);
   __syncthreads();
   const unsigned int tile = s_tile;
   const scl_u64 base = (scl_u64)tile * TILE;
@@ -227,43 +309,15 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
     scl_C prefix = (scl_C)ident;
     if (lane == 0) scl_publish(st, tile, tile == 0, aggc);
     if (tile != 0) {
-      scl_C running = (scl_C)ident;  // fold of the tiles already visited (later ones)
-      long long pred = (long long)tile - 1;
-      while (true) {
-        const long long idx = pred - lane;
-        scl_C v = (scl_C)ident;
-        int kind = 2;  // beyond tile 0: nothing to add, stop here
-        if (idx >= 0) {
-          kind = scl_poll(st, idx, spin_limit, &v);
-          if (kind == 0) {
-            scl_raise(err, SCL_DEV_ERR_TIMEOUT);
-            v = (scl_C)ident;
-            kind = 2;
-          }
-        }
-        const unsigned int pmask = __ballot_sync(0xffffffffu, kind == 2);
-        const int first = pmask ? __ffs(pmask) - 1 : 31;  // nearest inclusive prefix
-        if (lane > first) v = (scl_C)ident;
-        // ordered fold over lanes: higher lane = earlier tile
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-          scl_C o = scl_shfl_down(v, off);
-          if (lane + off < 32) v = (scl_C)SCL_FUNC_C(o, v SCL_OP_ARGS);
-        }
-        const scl_C window = scl_shfl_idx(v, 0);
-        running = (scl_C)SCL_FUNC_C(window, running SCL_OP_ARGS);
-        if (pmask) break;
-        pred -= 32;
-      }
-      prefix = running;
+      prefix = scl_lookback(st, (long long)tile, 0, spin_limit, err SCL_EXTRA_ARGS);
       if (lane == 0) scl_publish(st, tile, true, (scl_C)SCL_FUNC_C(prefix, aggc SCL_OP_ARGS));
     }
-    if (lane == 0) s_prefix = prefix;
+    if (lane == 0) s_carry = (scl_T)prefix;
   }
   __syncthreads();
 
   // ---- outputs (computed in place in x)
-  const scl_T tile_carry = (scl_T)s_prefix;
+  const scl_T tile_carry = s_carry;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     scl_T lane_excl = scl_shfl_up(wincl[r], 1);
@@ -349,7 +403,7 @@ __device__ __forceinline__ bool scl_mbar_wait(unsigned int bar_s, unsigned int s
 template <int R, int MINB, int SEG = 0>
 __global__ void __launch_bounds__(SCL_SCAN_B, MINB)
 scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int aligned,
-           unsigned int* tile_counter, scl_scan_status st, unsigned int spin_limit,
+           unsigned int* tile_counter, scl_scan_status st, scl_scan_clear clr, unsigned int spin_limit,
            unsigned int* err, const scl_u64* seg_off, const unsigned int* tile_start,
            scl_u64 n_seg SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
@@ -368,7 +422,7 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
   __shared__ unsigned int s_tile;
   __shared__ int s_ok;
   __shared__ scl_T s_wsum[R * W];
-  __shared__ scl_C s_prefix;
+  __shared__ scl_T s_carry;  // the tile's prefix, converted once to the element type
   const unsigned int bar_s = (unsigned int)__cvta_generic_to_shared(&bar);
   if (threadIdx.x == 0) {
     // segmented: the grid is an upper bound; blocks at or past the tile count
@@ -380,6 +434,7 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar_s));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  scl_scan_clear_other(clr);
   __syncthreads();
   const unsigned int tile = s_tile;
   unsigned int first = 0;  // ticket of the first tile of this tile's sequence
@@ -480,7 +535,7 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
   // ---- in-thread inclusive scan of each logical vector (written back to its
   //      slot in logical order), warp scans of the vector totals.  Logical
   //      vector q sits at q*V, or at TILE-(q+1)*V reversed for a reverse scan.
-  scl_T wincl[R];
+  scl_T wincl[R];  // (unused with local prefixes)
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int q = r * B + threadIdx.x;
@@ -503,9 +558,19 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
     }
 #pragma unroll
     for (int e = 1; e < V; ++e) p.v[e] = SCL_FUNC(p.v[e - 1], p.v[e] SCL_OP_ARGS);
-    scl_store<scl_T, V>(ts + pos, p);
-    wincl[r] = scl_warp_incl(p.v[V - 1] SCL_EXTRA_ARGS);
-    if (lane == 31) s_wsum[r * W + warp] = wincl[r];
+    if constexpr (kLocalPrefix) {
+      const scl_T tot = scl_warp_incl(p.v[V - 1] SCL_EXTRA_ARGS);
+      scl_T lx = scl_shfl_up(tot, 1);
+      if (lane == 0) lx = ident;
+      if (lane == 31) s_wsum[r * W + warp] = tot;
+#pragma unroll
+      for (int e = 0; e < V; ++e) p.v[e] = SCL_FUNC(lx, p.v[e] SCL_OP_ARGS);
+      scl_store<scl_T, V>(ts + pos, p);
+    } else {
+      scl_store<scl_T, V>(ts + pos, p);
+      wincl[r] = scl_warp_incl(p.v[V - 1] SCL_EXTRA_ARGS);
+      if (lane == 31) s_wsum[r * W + warp] = wincl[r];
+    }
   }
   __syncthreads();
 
@@ -527,42 +592,15 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
     scl_C prefix = (scl_C)ident;
     if (lane == 0) scl_publish(st, tile, tile == first, aggc);
     if (tile != first) {
-      scl_C running = (scl_C)ident;
-      long long pred = (long long)tile - 1;
-      while (true) {
-        const long long idx = pred - lane;
-        scl_C v = (scl_C)ident;
-        int kind = 2;  // before the sequence's first tile: nothing to add
-        if (idx >= (long long)first) {
-          kind = scl_poll(st, idx, spin_limit, &v);
-          if (kind == 0) {
-            scl_raise(err, SCL_DEV_ERR_TIMEOUT);
-            v = (scl_C)ident;
-            kind = 2;
-          }
-        }
-        const unsigned int pmask = __ballot_sync(0xffffffffu, kind == 2);
-        const int first_inc = pmask ? __ffs(pmask) - 1 : 31;
-        if (lane > first_inc) v = (scl_C)ident;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-          scl_C o = scl_shfl_down(v, off);
-          if (lane + off < 32) v = (scl_C)SCL_FUNC_C(o, v SCL_OP_ARGS);
-        }
-        const scl_C window = scl_shfl_idx(v, 0);
-        running = (scl_C)SCL_FUNC_C(window, running SCL_OP_ARGS);
-        if (pmask) break;
-        pred -= 32;
-      }
-      prefix = running;
+      prefix = scl_lookback(st, (long long)tile, (long long)first, spin_limit, err SCL_EXTRA_ARGS);
       if (lane == 0) scl_publish(st, tile, true, (scl_C)SCL_FUNC_C(prefix, aggc SCL_OP_ARGS));
     }
-    if (lane == 0) s_prefix = prefix;
+    if (lane == 0) s_carry = (scl_T)prefix;
   }
   __syncthreads();
 
   // ---- outputs: 16-byte stores for whole slots when `out` shares the grid
-  const scl_T tile_carry = (scl_T)s_prefix;
+  const scl_T tile_carry = s_carry;
   // (whole-slot stores need the output elements the size of the scanned ones)
   const bool ovec = sizeof(scl_O) == sizeof(scl_T) && full &&
                     (((scl_u64)out + (scl_u64)(tile_lo * (long long)sizeof(scl_O))) & 15u) == 0;
@@ -571,18 +609,32 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
     const int q = r * B + threadIdx.x;
     const int pos = reverse ? TILE - (q + 1) * V : q * V;
     scl_pack<scl_T, V> p = scl_load<scl_T, V>(ts + pos);
-    scl_T lane_excl = scl_shfl_up(wincl[r], 1);
-    if (lane == 0) lane_excl = ident;
-    const scl_T pre = SCL_FUNC(SCL_FUNC(tile_carry, s_wsum[r * W + warp] SCL_OP_ARGS),
-                               lane_excl SCL_OP_ARGS);
     scl_pack<scl_T, V> o;  // logical order
-    if (inclusive) {
+    if constexpr (kLocalPrefix) {
+      // the slot holds the warp-local inclusive values
+      const scl_T pre = SCL_FUNC(tile_carry, s_wsum[r * W + warp] SCL_OP_ARGS);
+      if (inclusive) {
 #pragma unroll
-      for (int e = 0; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e] SCL_OP_ARGS);
+        for (int e = 0; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e] SCL_OP_ARGS);
+      } else {
+        const scl_T lx = scl_shfl_up(p.v[V - 1], 1);  // the previous lane's last value
+        o.v[0] = lane == 0 ? pre : SCL_FUNC(pre, lx SCL_OP_ARGS);
+#pragma unroll
+        for (int e = 1; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e - 1] SCL_OP_ARGS);
+      }
     } else {
-      o.v[0] = pre;
+      scl_T lane_excl = scl_shfl_up(wincl[r], 1);
+      if (lane == 0) lane_excl = ident;
+      const scl_T pre = SCL_FUNC(SCL_FUNC(tile_carry, s_wsum[r * W + warp] SCL_OP_ARGS),
+                                 lane_excl SCL_OP_ARGS);
+      if (inclusive) {
 #pragma unroll
-      for (int e = 1; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e - 1] SCL_OP_ARGS);
+        for (int e = 0; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e] SCL_OP_ARGS);
+      } else {
+        o.v[0] = pre;
+#pragma unroll
+        for (int e = 1; e < V; ++e) o.v[e] = SCL_FUNC(pre, p.v[e - 1] SCL_OP_ARGS);
+      }
     }
     if (reverse) {  // back to physical order
 #pragma unroll
