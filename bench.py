@@ -41,6 +41,7 @@ MOD = 7919
 BYTES_SCAN = 2 * 4 * N_SCAN
 BYTES_MAP = 2 * 4 * N_SCAN
 METRIC = "HBM GB/s (int32 inclusive Scan + Map(x mod 7919), N=2^28)"
+WORKLOAD = "inclusive Scan(int32 +) over 2^28 then Map(x mod 7919)"
 
 
 def peaks():
@@ -292,7 +293,7 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "int32",
         "data": "synthetic (SplitMix64 seed 0, uniform {0..1000})",
-        "config": {"workload": "inclusive Scan(int32 +) over 2^28 then Map(x mod 7919)",
+        "config": {"workload": WORKLOAD,
                    "n": N_SCAN, "l2": "inputs (1 GiB) larger than L2; no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "parity": {"bit_exact_vs_oracle": parity},
@@ -310,7 +311,7 @@ def run_gpu(args):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(sample=1 << 26)
+        line["cpu_baseline"] = cpu_baseline(sample=N_SCAN)
     if rank == 0 and not args.headline_only:
         line["skeletons"] = secondary(S, oracle, hbm_peak, args)
     if rank == 0:
@@ -333,14 +334,47 @@ def cpu_baseline(sample: int, reps: int = 3):
         oracle.scan_incl_mod_i32_mt(x, MOD, nt, out)
         ts.append(time.perf_counter() - t)
     sec = statistics.median(ts)
+    whole = " (the whole workload)" if sample == N_SCAN else ""
     return {"value": round(16 * sample / sec / 1e9, 3), "unit": "GB/s", "cores": nt, "kind": "port",
-            "sample": f"2^{sample.bit_length() - 1} int32 (scan+mod fused, two-pass chunked), "
-                      f"median of {reps}"}
+            "sample": f"2^{sample.bit_length() - 1} int32{whole} per run (scan+mod fused, two-pass "
+                      f"chunked), median of {reps}"}
+
+
+def fp32_peak_measured(S, device: int = 0, seconds: float = 0.6):
+    """FP32 CUDA-core peak of this GPU, measured: the library's probe of 16
+    independent FMA chains per thread at 2048 threads per SM (scalar
+    fma.rn.f32, then packed fma.rn.f32x2), each timed with events on the
+    library stream for about `seconds`, the SM clock sampled meanwhile.  The
+    peak is the faster form's rate."""
+    L = S.lib()
+    sink = S.DeviceArray(1 << 21, np.float32)
+    res = {}
+    import ctypes
+    for name, packed in (("scalar_ffma", 0), ("packed_ffma2", 1)):
+        flops = ctypes.c_uint64(0)
+        iters = 4096
+
+        def fn():
+            S.check(L.scl_debug_fp32_peak(packed, iters, sink.ptr, 1 << 21, ctypes.byref(flops)))
+        ms1 = timed(S, fn, 3, 2)
+        reps = max(10, int(seconds * 1e3 / max(ms1, 1e-3)))
+        sampler = ClockSampler(device)
+        sampler.start()
+        ms = timed(S, fn, reps, 2)
+        clk = sampler.stop()
+        res[name] = {"TFLOPs": round(flops.value / ms / 1e9, 2), "ms": round(ms, 4), "launches": reps,
+                     "sm_mhz_median": clk.get("sm_mhz"), "clock_reasons": clk.get("reasons")}
+    peak = max(v["TFLOPs"] for v in res.values())
+    res["peak_TFLOPs"] = peak
+    res["note"] = ("dense FP32 FMA rate this GPU sustained at the sampled clock; the CUDA-core "
+                   "kernels' fp32_frac is against it")
+    return peak, res
 
 
 def secondary(S, oracle, hbm_peak, args):
     out = {}
-    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12  # nominal FP32 TFLOP/s (152 SMs x 128 lanes x FMA x 2.07 GHz)
+    fp32_peak, out["fp32_peak_measured"] = fp32_peak_measured(S)
+    bf16_peak = peaks()[1]
     # dot product: Zip(mult) then Reduce(add), N = 2^24
     n = 1 << 24
     a = oracle.uniform_f32(n, 0, -1.0, 1.0)
@@ -511,7 +545,7 @@ def secondary(S, oracle, hbm_peak, args):
         err = float(np.abs(do.to_numpy().reshape(rows, cols) - ref).max())
         del ref
         mo[name] = {"max_abs_err_vs_fp64": err, "GBps": round(gbps, 1), "hbm_frac": round(gbps / hbm_peak, 3),
-                    "TFLOPs": round(tflops, 2), "fp32_frac_nominal": round(tflops / fp32_peak, 3),
+                    "TFLOPs": round(tflops, 2), "fp32_frac": round(tflops / fp32_peak, 3),
                     "variant": p.last_variant, "adjoint_ms": round(a_ms, 4), "fwd_ms": round(ms, 4),
                     "fwd_plus_adjoint_over_fwd": round((ms + a_ms) / ms, 3)}
     out["mapoverlap_8192^2_R5"] = mo
@@ -539,6 +573,13 @@ def secondary(S, oracle, hbm_peak, args):
         err = np.abs(P[rows_chk].astype(np.float64) - ref)
         res[name] = {"ms": round(ms, 3), "TFLOPs": round(2 * M * N * K / ms / 1e9, 2),
                      "variant": ap.last_variant,
+                     # CUDA-core kernel: FP32 flops over the measured FP32 peak;
+                     # tensor cores: the bf16 products' flops over the bf16 peak
+                     "frac": round((2 * M * N * K if var == S.VARIANT_SIMT else
+                                    (6 if items == 3 else 3) * 2 * M * N * K) / ms / 1e9 /
+                                   (fp32_peak if var == S.VARIANT_SIMT else bf16_peak), 3),
+                     "frac_of": "measured FP32 peak" if var == S.VARIANT_SIMT else
+                                "bf16 burst peak (MEASURED_PEAKS.json), bf16 products' flops",
                      "normwise_err_vs_fp64": float(err.max() / np.abs(ref).max()),
                      "median_rel_err_vs_fp64": float(np.median(err / np.maximum(np.abs(ref), 1e-30)))}
     res["speedup_tc6_over_simt"] = round(res["fp32_simt"]["ms"] / res["tc_3xbf16_6prod"]["ms"], 2)
@@ -589,7 +630,7 @@ def secondary(S, oracle, hbm_peak, args):
     out["manhattan_4096x256x4096"] = {"ms": round(ms, 3),
                                        "Gpairops": round(Ml * Nl * Kl / ms / 1e6, 1),
                                        "TFLOPs_3flop": round(3 * Ml * Nl * Kl / ms / 1e9, 2),
-                                       "fp32_frac_nominal": round(3 * Ml * Nl * Kl / ms / 1e9 / fp32_peak, 3),
+                                       "fp32_frac": round(3 * Ml * Nl * Kl / ms / 1e9 / fp32_peak, 3),
                                        "normwise_err_vs_fp64": man_err,
                                        "generic_form": {
                                            "ms": round(gms, 3),
@@ -736,7 +777,7 @@ def run_reference(args):
     if rank != 0:
         return
     import oracle
-    n = 1 << 26  # bounded sample per step: 1/4 of the 2^28 workload
+    n = N_SCAN  # the whole 2^28 workload every step (about 60-70 ms on 16 host cores)
     x = oracle.mod_i32(n, 0, 1001)
     out = np.empty_like(x)
     nt = oracle.threads()
@@ -750,18 +791,19 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": "GB/s",
             "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(sec * 1e3, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int32", "data": "synthetic (SplitMix64 seed 0)",
-            "config": {"workload": "inclusive Scan(int32 +) then Map(x mod 7919)",
-                       "sample": "2^26 of the 2^28 elements per step"},
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (SplitMix64 seed 0, uniform {0..1000})",
+            "config": {"workload": WORKLOAD, "n": n, "l2": "inputs (1 GiB) larger than L2; no flush",
+                       "parallelism": "single host"},
             "cpu_baseline": {"value": round(val, 3), "unit": "GB/s", "cores": nt, "kind": "port",
-                             "sample": "2^26 int32 per step, scan+mod fused (two-pass chunked)"},
+                             "sample": "2^28 int32 (the whole workload) per step, scan+mod fused "
+                                       "(two-pass chunked)"},
             "e2e": {"value": round(val, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "SkelCL itself needs an OpenCL platform + libclang (absent); this is the oracle port"}
     print(json.dumps(line), flush=True)
 
 
 CASES = ("scan_int32", "map_mod", "zip_mul", "reduce_f32", "scan_f32", "mapoverlap", "allpairs_simt",
-         "allpairs_tc", "manhattan", "segmented_short")
+         "allpairs_tc", "manhattan", "segmented_short", "fp32_peak")
 
 
 def run_case(args):
@@ -772,6 +814,11 @@ def run_case(args):
     S.init(0)
     n = args.n
     c = args.case
+    if c == "fp32_peak":
+        peak, res = fp32_peak_measured(S)
+        print(json.dumps({"case": c, "rate": peak, "unit": "TFLOP/s", "detail": res,
+                          "launches": S.launch_count()}), flush=True)
+        return
     if c in ("scan_int32", "map_mod"):
         x = S.DeviceArray.from_numpy(oracle.mod_i32(n, 0, 1001))
         y = S.DeviceArray(n, np.int32)

@@ -7,7 +7,8 @@ known answer used here is literally present at the cited line, and writes the
 cases as data, so the oracle and the GPU path can be pinned against them on a
 machine without the reference sources.
 
-Run: python tests/golden/make_kats.py [path-to-reference]   (default /root/reference)
+Run: python tests/golden/make_kats.py [path-to-reference]
+     (default: the directory SKELCL_REFERENCE_DIR names)
 """
 from __future__ import annotations
 
@@ -106,4 +107,8 @@ def main(ref_root: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    import os
+    where = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SKELCL_REFERENCE_DIR")
+    if not where:
+        raise SystemExit("usage: make_kats.py PATH-TO-REFERENCE (or set SKELCL_REFERENCE_DIR)")
+    main(Path(where))

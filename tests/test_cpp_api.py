@@ -1,7 +1,9 @@
 """The drop-in C++ API (include/SkelCL): the reference's own gtest sources
-for the skeleton path compile unchanged against these headers (CPU, when the
-reference sources are present), and the known-answer port in
-tests/cpp/skelcl_api_tests.cpp builds here and passes on the GPU."""
+for the skeleton path compile and link unchanged against these headers and
+libskelcl_cuda.so (CPU; SKELCL_REFERENCE_DIR names the reference checkout,
+and these cases skip without it), its SHA-1 suite runs unchanged here, and
+the known-answer port in tests/cpp/skelcl_api_tests.cpp builds here and
+passes on the GPU."""
 import os
 import shutil
 import subprocess
@@ -10,7 +12,8 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
-REF = Path("/root/reference")
+REF = Path(os.environ["SKELCL_REFERENCE_DIR"]) if os.environ.get("SKELCL_REFERENCE_DIR") else None
+HAVE_REF = REF is not None and (REF / "test").is_dir()
 CXX = shutil.which("g++") or "g++"
 HOT_PATH_SUITES = ["MapTests", "ZipTests", "ReduceTests", "ScanTests", "MapOverlapTests",
                    "AllPairsTests", "IndexVectorTests", "IndexMatrixTests", "SHA1Tests",
@@ -26,13 +29,32 @@ def build_port(out: Path, source: str = "skelcl_api_tests.cpp") -> None:
     assert r.returncode == 0, r.stderr[-4000:]
 
 
-@pytest.mark.skipif(not REF.exists(), reason="reference sources not present")
-@pytest.mark.parametrize("suite", HOT_PATH_SUITES)
-def test_reference_suite_compiles_unchanged(built, suite):
-    src = REF / "test" / f"{suite}.cpp"
-    r = subprocess.run([CXX, "-std=c++17", "-fsyntax-only", f"-I{ROOT / 'include'}",
-                        f"-I{ROOT / 'tests' / 'cpp'}", str(src)], capture_output=True, text=True)
+def link_reference_suite(suite: str, out: Path) -> None:
+    """One unchanged reference test file + the gtest-compatible harness's
+    main(), linked against libskelcl_cuda.so: a symbol the headers declare
+    but nothing defines fails here, as it would in the reference's build
+    (test/CMakeLists.txt:12-33 links each suite with gtest_main)."""
+    lib = ROOT / "skelcl_gb300"
+    cmd = [CXX, "-std=c++17", "-O0", f"-I{ROOT / 'include'}", f"-I{ROOT / 'tests' / 'cpp'}",
+           str(REF / "test" / f"{suite}.cpp"), str(ROOT / "tests" / "cpp" / "gtest_main.cpp"),
+           f"-L{lib}", "-lskelcl_cuda", f"-Wl,-rpath,{lib}", "-o", str(out)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
+
+
+@pytest.mark.skipif(not HAVE_REF, reason="SKELCL_REFERENCE_DIR does not name the reference sources")
+@pytest.mark.parametrize("suite", HOT_PATH_SUITES)
+def test_reference_suite_links_unchanged(built, tmp_path, suite):
+    link_reference_suite(suite, tmp_path / suite)
+
+
+@pytest.mark.skipif(not HAVE_REF, reason="SKELCL_REFERENCE_DIR does not name the reference sources")
+def test_reference_sha1_suite_passes_unchanged(built, tmp_path):
+    """The one suite that needs no device runs here, unchanged."""
+    exe = tmp_path / "SHA1Tests"
+    link_reference_suite("SHA1Tests", exe)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and "3 tests ran, 0 failed." in r.stdout, r.stdout + r.stderr
 
 
 def test_api_port_builds(built, tmp_path):

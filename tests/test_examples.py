@@ -1,6 +1,7 @@
-"""Examples as drivers: the reference's example programs compile unchanged
-against include/SkelCL and include/pvsutil (CPU, where the reference sources
-are present); this repository's examples/ build and, on the GPU, run with
+"""Examples as drivers: the reference's example programs compile and link
+unchanged against include/SkelCL, include/pvsutil and libskelcl_cuda.so
+(CPU; SKELCL_REFERENCE_DIR names the reference checkout, and these cases skip
+without it); this repository's examples/ build and, on the GPU, run with
 --check against host loops."""
 import os
 import shutil
@@ -10,7 +11,8 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
-REF = Path("/root/reference")
+REF = Path(os.environ["SKELCL_REFERENCE_DIR"]) if os.environ.get("SKELCL_REFERENCE_DIR") else None
+HAVE_REF = REF is not None and (REF / "examples").is_dir()
 CXX = shutil.which("g++") or "g++"
 OURS = ["dot_product", "saxpy", "gauss", "matrix_mult", "mandelbrot"]
 RUN_ARGS = {"dot_product": ["-n", "1000003"], "saxpy": ["-n", "100003"], "gauss": ["-r", "5"],
@@ -25,11 +27,13 @@ def build(name: str, out: Path) -> None:
     assert r.returncode == 0, r.stderr[-4000:]
 
 
-@pytest.mark.skipif(not REF.exists(), reason="reference sources not present")
+@pytest.mark.skipif(not HAVE_REF, reason="SKELCL_REFERENCE_DIR does not name the reference sources")
 @pytest.mark.parametrize("example", ["dot_product", "gauss", "mandelbrot", "matrix_mult", "montecarlo", "saxpy"])
-def test_reference_example_compiles_unchanged(built, example):
-    r = subprocess.run([CXX, "-std=c++17", "-fsyntax-only", f"-I{ROOT / 'include'}",
-                        str(REF / "examples" / example / "main.cpp")], capture_output=True, text=True)
+def test_reference_example_links_unchanged(built, tmp_path, example):
+    lib = ROOT / "skelcl_gb300"
+    r = subprocess.run([CXX, "-std=c++17", "-O0", f"-I{ROOT / 'include'}",
+                        str(REF / "examples" / example / "main.cpp"), f"-L{lib}", "-lskelcl_cuda",
+                        f"-Wl,-rpath,{lib}", "-o", str(tmp_path / example)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
 
 
