@@ -392,6 +392,24 @@ def secondary(S, oracle, hbm_peak, args):
                    source2="float m(float x, float y){ return x*y; }", func2="m", identity="0")
     fms = timed(S, lambda: zr.launch([da, db, dr], n=n), 20, 3)
     fdot = float(dr.to_numpy()[0])
+    # the same with the inputs rotating through four pairs (1 GiB of inputs,
+    # more than L2): consecutive iterations find nothing of theirs in L2, so
+    # these are HBM figures
+    pairs = [(da, db)] + [(S.DeviceArray.from_numpy(oracle.uniform_f32(n, 10 + 2 * k, -1.0, 1.0)),
+                           S.DeviceArray.from_numpy(oracle.uniform_f32(n, 11 + 2 * k, -1.0, 1.0)))
+                          for k in range(3)]
+    zs = [dz] + [S.DeviceArray(n, np.float32) for _ in range(3)]
+    it = {"k": 0}
+
+    def rot(fn):
+        def step():
+            k = it["k"] = (it["k"] + 1) % 4
+            fn(k)
+        return step
+    zms_h = timed(S, rot(lambda k: zp.launch([pairs[k][0], pairs[k][1], zs[k]], n=n)), 20, 4)
+    rms_h = timed(S, rot(lambda k: rp.launch([zs[k], dr], n=n)), 20, 4)
+    fms_h = timed(S, rot(lambda k: zr.launch([pairs[k][0], pairs[k][1], dr], n=n)), 20, 4)
+    del pairs, zs
     out["dot_product_2^24"] = {
         "zip_GBps": round(12 * n / zms / 1e6, 1), "reduce_GBps": round(4 * n / rms / 1e6, 1),
         "zip_frac": round(12 * n / zms / 1e6 / hbm_peak, 3),
@@ -400,7 +418,15 @@ def secondary(S, oracle, hbm_peak, args):
         "fused_zip_reduce": {"ms": round(fms, 4), "GBps": round(8 * n / fms / 1e6, 1),
                              "unfused_ms": round(zms + rms, 4), "speedup": round((zms + rms) / fms, 2),
                              "rel_err_vs_fp64": abs(fdot - ref) / abs(ref)},
-        "note": "inputs 128 MiB, about L2 size: figures include L2 reuse across iterations"}
+        "hbm": {"zip_GBps": round(12 * n / zms_h / 1e6, 1), "zip_frac": round(12 * n / zms_h / 1e6 / hbm_peak, 3),
+                "reduce_GBps": round(4 * n / rms_h / 1e6, 1),
+                "reduce_frac": round(4 * n / rms_h / 1e6 / hbm_peak, 3),
+                "fused_ms": round(fms_h, 4), "fused_GBps": round(8 * n / fms_h / 1e6, 1),
+                "fused_frac": round(8 * n / fms_h / 1e6 / hbm_peak, 3),
+                "unfused_ms": round(zms_h + rms_h, 4),
+                "note": "inputs rotating through four pairs (1 GiB): no L2 reuse between iterations"},
+        "note": "top-level figures: the same 128 MiB of inputs every iteration (about L2 size, "
+                "so they include L2 reuse); 'hbm': rotating inputs"}
     del da, db, dz, dr
 
     # Map / Zip / Reduce at 2^26 and their adjoints (the user's vector-Jacobian
@@ -563,11 +589,14 @@ def secondary(S, oracle, hbm_peak, args):
     ref = oracle.gemm_f64(A.reshape(M, K)[rows_chk], B.reshape(K, N))
     # the tensor-core launches take 128 x 256 output tiles here (automatic
     # choice); "_128col" repeats the 6-product one with 128 x 128 tiles
-    for name, var, items, cols in (("fp32_simt", S.VARIANT_SIMT, 0, 0),
-                                   ("tc_3xbf16_6prod", S.VARIANT_TC3XBF16, 3, 0),
-                                   ("tc_3xbf16_6prod_128col", S.VARIANT_TC3XBF16, 3, 128),
-                                   ("tc_3xbf16_3prod", S.VARIANT_TC3XBF16, 2, 0)):
-        tun = S.Tuning(variant=var, items=items, tile_h=cols)
+    # (the tensor-core tiles are taken in groups of 16 tile rows; "_rowmajor"
+    # repeats the 6-product launch in plain row-major tile order)
+    for name, var, items, cols, group in (("fp32_simt", S.VARIANT_SIMT, 0, 0, 0),
+                                          ("tc_3xbf16_6prod", S.VARIANT_TC3XBF16, 3, 0, 0),
+                                          ("tc_3xbf16_6prod_rowmajor", S.VARIANT_TC3XBF16, 3, 0, 1),
+                                          ("tc_3xbf16_6prod_128col", S.VARIANT_TC3XBF16, 3, 128, 0),
+                                          ("tc_3xbf16_3prod", S.VARIANT_TC3XBF16, 2, 0, 0)):
+        tun = S.Tuning(variant=var, items=items, tile_h=cols, workgroup=group)
         ms = timed(S, lambda: ap.launch([dA, dB, dP], rows=M, cols=N, dim=K, tuning=tun), 3, 1)
         P = dP.to_numpy().reshape(M, N)
         err = np.abs(P[rows_chk].astype(np.float64) - ref)
@@ -582,6 +611,21 @@ def secondary(S, oracle, hbm_peak, args):
                                 "bf16 burst peak (MEASURED_PEAKS.json), bf16 products' flops",
                      "normwise_err_vs_fp64": float(err.max() / np.abs(ref).max()),
                      "median_rel_err_vs_fp64": float(np.median(err / np.maximum(np.abs(ref), 1e-30)))}
+    # the split pass alone (both operands into bf16 planes), which every
+    # tensor-core launch above includes
+    import ctypes
+    for name, parts in (("tc_3xbf16_6prod", 3), ("tc_3xbf16_3prod", 2)):
+        need = ctypes.c_size_t(0)
+        S.check(S.lib().scl_debug_allpairs_split(None, None, M, N, K, parts, 0, None, 0, ctypes.byref(need)))
+        scratch = S.DeviceArray((need.value + 15) // 16 * 4, np.float32)
+        sms = timed(S, lambda: S.check(S.lib().scl_debug_allpairs_split(
+            dA.ptr, dB.ptr, M, N, K, parts, 0, scratch.ptr, scratch.n * 4, None)), 5, 2)
+        del scratch
+        res[name]["split_ms"] = round(sms, 3)
+        res[name]["contraction_ms"] = round(res[name]["ms"] - sms, 3)
+        prods = 6 if parts == 3 else 3
+        res[name]["contraction_frac_of_bf16_peak"] = round(
+            prods * 2 * M * N * K / (res[name]["ms"] - sms) / 1e9 / bf16_peak, 3)
     res["speedup_tc6_over_simt"] = round(res["fp32_simt"]["ms"] / res["tc_3xbf16_6prod"]["ms"], 2)
     res["speedup_tc3_over_simt"] = round(res["fp32_simt"]["ms"] / res["tc_3xbf16_3prod"]["ms"], 2)
     # backward of L = sum(G * P) as two AllPairs on transposed operands (tensor cores)
@@ -655,20 +699,28 @@ def segmented_short(S, oracle, hbm_peak):
     rp = S.Program(S.KIND_REDUCE, "float func(float x, float y){ return x+y; }", ["float"], identity="0")
     dx, dy, dr, doff = (S.DeviceArray.from_numpy(x), S.DeviceArray(n, np.float32),
                         S.DeviceArray(nseg, np.float32), S.DeviceArray.from_numpy(off))
-    seg_scan = timed(S, lambda: sp.launch([dx, dy], n=n, flags=S.SHAPE_INCLUSIVE, segments=doff), 10, 3)
-    seg_red = timed(S, lambda: rp.launch([dx, dr], n=n, segments=doff), 10, 3)
+    plan = S.SegPlan(doff, n)
+    # with the plan (one launch per skeleton call), then without it (the
+    # offsets pre-pass and separate short / tiled launches on every call)
+    seg_scan = timed(S, lambda: sp.launch([dx, dy], n=n, flags=S.SHAPE_INCLUSIVE, segments=plan), 10, 3)
+    seg_red = timed(S, lambda: rp.launch([dx, dr], n=n, segments=plan), 10, 3)
+    np_scan = timed(S, lambda: sp.launch([dx, dy], n=n, flags=S.SHAPE_INCLUSIVE, segments=doff), 10, 3)
+    np_red = timed(S, lambda: rp.launch([dx, dr], n=n, segments=doff), 10, 3)
+    rp.launch([dx, dr], n=n, segments=plan)
     sums = dr.to_numpy().astype(np.float64)
     pick = np.arange(0, nseg, nseg // 1000)
     ref = np.array([oracle.sum_f64(x[int(off[i]):int(off[i + 1])]) for i in pick])
     flat_scan = timed(S, lambda: sp.launch([dx, dy], n=n, flags=S.SHAPE_INCLUSIVE), 10, 3)
     flat_red = timed(S, lambda: rp.launch([dx, dr], n=n), 10, 3)
+    plan.release()
     return {"n_vectors": nseg, "elements": n,
             "scan": {"ms": round(seg_scan, 4), "GBps": round(8 * n / seg_scan / 1e6, 1),
-                     "flat_ms": round(flat_scan, 4)},
+                     "flat_ms": round(flat_scan, 4), "without_plan_ms": round(np_scan, 4)},
             "reduce": {"ms": round(seg_red, 4), "GBps": round(4 * n / seg_red / 1e6, 1),
-                       "flat_ms": round(flat_red, 4),
+                       "flat_ms": round(flat_red, 4), "without_plan_ms": round(np_red, 4),
                        "max_abs_err_vs_fp64_sampled": float(np.abs(sums[pick] - ref).max())},
-            "note": "vectors of up to 4096 elements take one warp each; longer ones tiles"}
+            "note": "with a segment plan: one launch per call, vectors of up to 4096 elements a "
+                    "warp each; without it the offsets pre-pass runs on every call"}
 
 
 def segmented(S, oracle, hbm_peak):
@@ -676,7 +728,8 @@ def segmented(S, oracle, hbm_peak):
     U[-1,1] (seed 13), back to back: Map(x*x+1) -> inclusive Scan(+) ->
     Reduce(+) per vector, and the adjoints (segmented broadcast, segmented
     reverse scan, Map's vector-Jacobian product).  One launch per skeleton
-    (plus the offsets pre-pass) for all vectors, replayed from a CUDA graph;
+    for all vectors (a segment plan: the offsets pre-pass ran once, before),
+    replayed from a CUDA graph;
     against the same pipeline on one flat vector of the same length and
     against one launch per vector per skeleton (also replayed from a graph,
     so host overhead is not counted)."""
@@ -699,6 +752,7 @@ def segmented(S, oracle, hbm_peak):
     dr = S.DeviceArray(nseg, np.float32)
     dseed = S.DeviceArray.from_numpy(np.ones(nseg, np.float32))
     flat = S.DeviceArray.from_numpy(np.array([0, n], np.uint64))
+    plan, flat_plan = S.SegPlan(doff, n), S.SegPlan(flat, n)
 
     def fwd(segs, out):
         mp.launch([dx, dm], n=n)
@@ -706,7 +760,8 @@ def segmented(S, oracle, hbm_peak):
         rp.launch([ds, out], n=n, segments=segs)
 
     def adj(segs, nsegs):
-        S.check(L.scl_adjoint_broadcast_segments(dseed.ptr, dgs.ptr, segs.ptr, nsegs, n, S.DTYPE_F32, 0))
+        offs = segs.offsets if isinstance(segs, S.SegPlan) else segs
+        S.check(L.scl_adjoint_broadcast_segments(dseed.ptr, dgs.ptr, offs.ptr, nsegs, n, S.DTYPE_F32, 0))
         sp.launch([dgs, dgm], n=n, flags=S.SHAPE_INCLUSIVE | S.SHAPE_REVERSE, segments=segs)
         ma.launch([dx, dgm, dgx], n=n)
 
@@ -724,23 +779,26 @@ def segmented(S, oracle, hbm_peak):
 
     res = {"n_vectors": nseg, "elements": n, "mean_length": round(n / nseg, 1),
            "bytes_per_elem_fwd_adjoint": [20, 24]}
-    g_fwd = graph_of(lambda: fwd(doff, dr))
-    g_adj = graph_of(lambda: adj(doff, nseg))
+    g_fwd = graph_of(lambda: fwd(plan, dr))
+    g_adj = graph_of(lambda: adj(plan, nseg))
     dr1 = S.DeviceArray(1, np.float32)
-    g_flat_fwd = graph_of(lambda: fwd(flat, dr1))
-    g_flat_adj = graph_of(lambda: adj(flat, 1))
+    g_flat_fwd = graph_of(lambda: fwd(flat_plan, dr1))
+    g_flat_adj = graph_of(lambda: adj(flat_plan, 1))
+    g_np_fwd = graph_of(lambda: fwd(doff, dr))  # without the plan: the pre-pass on every call
     f_ms, a_ms = time_graph(g_fwd, 10), time_graph(g_adj, 10)
     ff_ms, fa_ms = time_graph(g_flat_fwd, 10), time_graph(g_flat_adj, 10)
+    np_ms = time_graph(g_np_fwd, 10)
     res["segmented"] = {"fwd_ms": round(f_ms, 3), "adjoint_ms": round(a_ms, 3),
                         "fwd_GBps": round(20 * n / f_ms / 1e6, 1), "adjoint_GBps": round(24 * n / a_ms / 1e6, 1),
                         "fwd_frac": round(20 * n / f_ms / 1e6 / hbm_peak, 3),
-                        "fwd_plus_adjoint_over_fwd": round((f_ms + a_ms) / f_ms, 3)}
+                        "fwd_plus_adjoint_over_fwd": round((f_ms + a_ms) / f_ms, 3),
+                        "fwd_ms_without_plan": round(np_ms, 3)}
     res["single_flat_vector"] = {"fwd_ms": round(ff_ms, 3), "adjoint_ms": round(fa_ms, 3),
                                  "fwd_GBps": round(20 * n / ff_ms / 1e6, 1),
                                  "adjoint_GBps": round(24 * n / fa_ms / 1e6, 1)}
     res["segmented_over_single_bandwidth"] = {"fwd": round(ff_ms / f_ms, 3), "adjoint": round(fa_ms / a_ms, 3)}
     # correctness on a sample of vectors (FP64)
-    fwd(doff, dr)
+    fwd(plan, dr)
     got = dr.to_numpy()
     chk = np.arange(0, nseg, 97)
     err = 0.0
@@ -749,7 +807,7 @@ def segmented(S, oracle, hbm_peak):
         v = np.cumsum(x[a:b].astype(np.float64) ** 2 + 1.0).sum()
         err = max(err, abs(float(got[s_]) - v) / abs(v))
     res["max_rel_err_vs_fp64_sampled"] = err
-    for g in (g_fwd, g_adj, g_flat_fwd, g_flat_adj):
+    for g in (g_fwd, g_adj, g_flat_fwd, g_flat_adj, g_np_fwd):
         L.scl_graph_destroy(g)
     # one launch per vector per skeleton, from a graph (forward only)
     views = [(dx.view(int(off[i]), int(lens[i])), dm.view(int(off[i]), int(lens[i])),
@@ -841,9 +899,11 @@ def run_case(args):
         sp = S.Program(S.KIND_SCAN, "float func(float x, float y){ return x+y; }", ["float"], identity="0")
         rp = S.Program(S.KIND_REDUCE, "float func(float x, float y){ return x+y; }", ["float"], identity="0")
 
+        plan = S.SegPlan(doff, ne)
+
         def fn():
-            sp.launch([a, z], n=ne, flags=S.SHAPE_INCLUSIVE, segments=doff)
-            rp.launch([a, r], n=ne, segments=doff)
+            sp.launch([a, z], n=ne, flags=S.SHAPE_INCLUSIVE, segments=plan)
+            rp.launch([a, r], n=ne, segments=plan)
         nbytes = 12 * ne
     elif c in ("zip_mul", "reduce_f32", "scan_f32"):
         a = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 0, -1.0, 1.0))

@@ -417,6 +417,7 @@ public:
       scl_shape sh = skelcl::detail::makeShape(in.size());
       sh.seg_offsets = segments.devicePtr();
       sh.n_segments = ns;
+      sh.seg_plan = segments.plan();
       detail::check(scl_launch_reduce(_fwd.get(), &sh, bufs, nullptr, 0, nullptr), "ad::Reduce::segmented");
       o.dataOnDeviceModified();
     }
@@ -511,6 +512,7 @@ public:
         sh.flags = _inclusive ? SCL_SHAPE_INCLUSIVE : 0u;
         sh.seg_offsets = segments.devicePtr();
         sh.n_segments = segments.count();
+        sh.seg_plan = segments.plan();
         detail::check(scl_launch_scan(_fwd.get(), &sh, bufs, nullptr, 0, nullptr), "ad::Scan::segmented");
       }
       o.dataOnDeviceModified();
@@ -533,6 +535,7 @@ public:
           s.flags = flags;
           s.seg_offsets = segs.devicePtr();
           s.n_segments = segs.count();
+          s.seg_plan = segs.plan();
           detail::check(scl_launch_scan(prog.get(), &s, b, nullptr, 0, nullptr), "ad::Scan::segmented adjoint");
         });
       });

@@ -76,6 +76,7 @@ public:
     scl_shape sh = detail::makeShape(input.size());
     sh.seg_offsets = segments.devicePtr();
     sh.n_segments = segments.count();
+    sh.seg_plan = segments.plan();
     scl_tuning t = tuning();
     launched(scl_launch_reduce(_program.get(), &sh, bufs, blob.data(), blob.size(), &t), "Reduce");
     o.dataOnDeviceModified();

@@ -79,6 +79,7 @@ public:
     sh.flags = (_inclusive ? SCL_SHAPE_INCLUSIVE : 0u) | (_reverse ? SCL_SHAPE_REVERSE : 0u);
     sh.seg_offsets = segments.devicePtr();
     sh.n_segments = segments.count();
+    sh.seg_plan = segments.plan();
     scl_tuning t = tuning();
     launched(scl_launch_scan(_program.get(), &sh, bufs, blob.data(), blob.size(), &t), "Scan");
     o.dataOnDeviceModified();

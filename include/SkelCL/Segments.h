@@ -6,6 +6,7 @@
 #define SKELCL_SEGMENTS_H_
 
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 #include <pvsutil/Assert.h>
@@ -34,9 +35,25 @@ public:
   // total number of elements (the last offset)
   size_t total() const { return _offsets.size() ? (size_t)_offsets.back() : 0; }
   const uint64_t* devicePtr() const { return _offsets.devicePtr(); }
+  // The segment plan of these offsets (scl_segplan_create), made on first
+  // use and shared by copies: with it a segmented Scan or Reduce is one
+  // launch and the offsets pre-pass runs once, not on every call.  The
+  // offsets never change after construction, so the plan stays valid.
+  uint32_t plan() const {
+    if (!_plan && count()) {
+      uint32_t id = 0;
+      if (scl_segplan_create(devicePtr(), count(), total(), &id) == SCL_OK && id)
+        _plan = std::shared_ptr<uint32_t>(new uint32_t(id), [](uint32_t* p) {
+          scl_segplan_release(*p);
+          delete p;
+        });
+    }
+    return _plan ? *_plan : 0u;
+  }
 
 private:
   Vector<uint64_t> _offsets;
+  mutable std::shared_ptr<uint32_t> _plan;
 };
 
 }  // namespace skelcl

@@ -128,7 +128,10 @@ typedef struct scl_shape {
                             element-wise: segments do not change them.  No
                             counterpart in the reference.                     */
   uint32_t flags;        /* SCL_SHAPE_* below                                 */
-  uint32_t reserved;
+  uint32_t seg_plan;     /* 0, or a segment plan (scl_segplan_create) made for
+                            these offsets and n_segments (and a length up to
+                            n): the segmented Scan or Reduce is then one
+                            launch, without the offsets pre-pass             */
 } scl_shape;
 
 #define SCL_SHAPE_INCLUSIVE 0x1u  /* Scan: inclusive instead of exclusive     */
@@ -144,7 +147,9 @@ typedef struct scl_shape {
  * default.  workgroup mirrors Skeleton::setWorkGroupSize (src/Skeleton.cpp:75-78). */
 /* Launch shape; a zero field takes the default. */
 typedef struct scl_tuning {
-  uint32_t workgroup;    /* threads per block (Map/Zip/Reduce)                */
+  uint32_t workgroup;    /* threads per block (Map/Zip/Reduce); AllPairs
+                            tensor cores: output-tile rows per group of the
+                            tile order (0: 16)                                */
   uint32_t items;        /* 16-byte vectors per thread (Map/Zip/Reduce/Scan);
                             AllPairs tensor cores: bf16 parts, 2 or 3          */
   uint32_t tile_w;       /* Scan: tiles per SM; AllPairs tensor cores:
@@ -309,6 +314,24 @@ int scl_launch_scan_noalloc(scl_program* prog, const scl_shape* shape,
                             void* const* buffers, const void* extra,
                             size_t extra_bytes, const scl_tuning* tuning);
 
+/* ---- segment plans (no counterpart in the reference): the offsets pre-pass
+ *      of segmented Scan and Reduce, done once per offsets array instead of
+ *      on every call.  scl_segplan_create copies `seg_offsets` (DEVICE,
+ *      n_segments + 1 entries, for a flat vector of n elements), clamps them
+ *      as a segmented launch would (bad offsets are reported by the next
+ *      scl_sync) and returns a plan id.  A shape with seg_plan = that id (the
+ *      same n_segments, and n at least the plan's) runs its segmented Scan or
+ *      Reduce as ONE
+ *      launch: the tiles of the long segments first, then a warp per segment
+ *      of up to 4096 elements.  The plan keeps, per tile shape, which tiles
+ *      belong to which segment; the first launch with a tile shape builds
+ *      that (three small launches and a read-back of the tile count), so make
+ *      it before capturing a graph.  Later changes to the caller's offsets
+ *      are not seen: release the plan and create another. */
+int scl_segplan_create(const uint64_t* seg_offsets, uint64_t n_segments, uint64_t n,
+                       uint32_t* plan);
+int scl_segplan_release(uint32_t plan);
+
 /* ---- adjoint building blocks (no counterpart in the reference; used by the
  *      reverse-mode tape in include/SkelCL/Adjoint.h).  Element types:   */
 enum scl_dtype { SCL_DTYPE_F32 = 1, SCL_DTYPE_F64 = 2 };
@@ -356,6 +379,14 @@ int scl_debug_counters(uint64_t* device_allocs, uint64_t* module_loads);
  * count; time it with events on the library stream. */
 int scl_debug_fp32_peak(int packed, uint32_t iters, float* sink, uint64_t sink_floats,
                         uint64_t* flops);
+/* The split pass of the tensor-core AllPairs alone (no counterpart in the
+ * reference): A (M x K) and B (K x N), or their transposes per the
+ * SCL_SHAPE_TRANS_* bits in `trans` (bit 0 left, bit 1 right), into `parts`
+ * bf16 planes in `scratch`; with scratch NULL only *needed is set.  For
+ * timing the split apart from the contraction. */
+int scl_debug_allpairs_split(const float* A, const float* B, uint32_t M, uint32_t N,
+                             uint32_t K, int parts, int trans, void* scratch,
+                             size_t scratch_bytes, size_t* needed);
 
 /* ---- CUDA graphs (no reference counterpart: skeleton sequences captured
  *      from the library stream and replayed with one launch). */

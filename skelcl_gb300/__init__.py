@@ -60,7 +60,7 @@ class Shape(ctypes.Structure):
     _fields_ = [("n", ctypes.c_uint64), ("rows", ctypes.c_uint64), ("cols", ctypes.c_uint64),
                 ("dim", ctypes.c_uint64), ("offset", ctypes.c_uint64),
                 ("seg_offsets", ctypes.c_void_p), ("n_segments", ctypes.c_uint64),
-                ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32), ("seg_plan", ctypes.c_uint32)]
 
 
 class Tuning(ctypes.Structure):
@@ -93,6 +93,8 @@ SIGNATURES = {
     "scl_program_last_variant": ([_VP, ctypes.POINTER(_U32)], _I),
     "scl_sha1_hex": ([_VP, _SZ, ctypes.c_char_p], _I),
     "scl_cache_stats": ([ctypes.POINTER(ctypes.c_uint64)] * 4, _I),
+    "scl_segplan_create": ([_VP, _U64, _U64, ctypes.POINTER(_U32)], _I),
+    "scl_segplan_release": ([_U32], _I),
     "scl_launch_map": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_zip": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_reduce": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
@@ -103,6 +105,7 @@ SIGNATURES = {
     "scl_launch_count": ([ctypes.POINTER(_U64)], _I),
     "scl_debug_counters": ([ctypes.POINTER(_U64), ctypes.POINTER(_U64)], _I),
     "scl_debug_fp32_peak": ([_I, _U32, _VP, _U64, ctypes.POINTER(_U64)], _I),
+    "scl_debug_allpairs_split": ([_VP, _VP, _U32, _U32, _U32, _I, _I, _VP, _SZ, ctypes.POINTER(_SZ)], _I),
     "scl_graph_begin": ([], _I), "scl_graph_end": ([ctypes.POINTER(_VP)], _I),
     "scl_graph_launch": ([_VP], _I), "scl_graph_destroy": ([_VP], _I),
     "scl_debug_bounded_wait": ([_U32, ctypes.POINTER(_I)], _I),
@@ -321,6 +324,29 @@ _LAUNCH = {KIND_MAP: "scl_launch_map", KIND_MAP_VOID: "scl_launch_map",
            KIND_ZIP_REDUCE: "scl_launch_reduce", KIND_SCAN_MAP: "scl_launch_scan"}
 
 
+class SegPlan:
+    """A segment plan (scl_segplan_create) for a DeviceArray of n_segments+1
+    uint64 offsets over a flat vector of n elements: segmented Scan and
+    Reduce launches given it run as one kernel each."""
+
+    def __init__(self, offsets: "DeviceArray", n: int):
+        self.offsets, self.n = offsets, n
+        pid = ctypes.c_uint32(0)
+        check(lib().scl_segplan_create(offsets.ptr, offsets.n - 1, n, ctypes.byref(pid)))
+        self.id = pid.value
+
+    def release(self) -> None:
+        if getattr(self, "id", 0):
+            lib().scl_segplan_release(self.id)
+            self.id = 0
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
 class Program:
     """A built skeleton program (one NVRTC module)."""
 
@@ -336,13 +362,18 @@ class Program:
 
     def launch(self, bufs: Iterable, n: int = 0, rows: int = 0, cols: int = 0, dim: int = 0,
                offset: int = 0, flags: int = 0, extra: bytes = b"",
-               tuning: Optional[Tuning] = None, segments: Optional["DeviceArray"] = None) -> None:
-        """`segments`: a DeviceArray of n_segments+1 uint64 offsets (segmented Scan/Reduce)."""
+               tuning: Optional[Tuning] = None, segments=None) -> None:
+        """`segments`: a DeviceArray of n_segments+1 uint64 offsets, or a
+        SegPlan made for them (segmented Scan/Reduce)."""
         ptrs = [b.ptr if isinstance(b, DeviceArray) else (b or 0) for b in bufs]
         arr = (ctypes.c_void_p * max(1, len(ptrs)))(*ptrs)
+        plan = 0
+        if isinstance(segments, SegPlan):
+            plan, segments = segments.id, segments.offsets
         sh = Shape(n=n, rows=rows, cols=cols, dim=dim, offset=offset,
                    seg_offsets=segments.ptr if segments is not None else None,
-                   n_segments=(segments.n - 1) if segments is not None else 0, flags=flags, reserved=0)
+                   n_segments=(segments.n - 1) if segments is not None else 0, flags=flags,
+                   seg_plan=plan)
         eb = ctypes.create_string_buffer(extra, len(extra)) if extra else None
         fn = getattr(lib(), _LAUNCH[self.kind])
         check(fn(self.handle, ctypes.byref(sh), arr, eb, len(extra),

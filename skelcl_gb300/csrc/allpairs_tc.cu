@@ -158,11 +158,19 @@ __global__ void split_transpose_kernel(const float* __restrict__ B, uint32_t K, 
 // G = k-blocks accumulated in tensor memory between two drains into the
 // epilogue's FP32 registers (1: every k-block; larger G drains less often at
 // a longer in-TMEM accumulation chain).
+//
+// Output tiles are numbered in groups of `group_m` tile rows: block b of the
+// 1D grid takes tile row first + (b mod group) mod rows and tile column
+// (b mod group) div rows of its group, so consecutive blocks share one
+// column of B's parts while cycling over a few rows of A's.  A wave of one
+// block per SM then reads about group_m rows of A and SMs / group_m columns
+// of B, which stay in L2 for the whole wave (row-major order read every
+// column of B in every wave: at 4096^3, 2.5x the parts' bytes from DRAM).
 template <int PARTS, int STAGES, int G, int BN_T>
 __global__ void __launch_bounds__(Shape<BN_T>::THREADS, 1)
 gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    float* __restrict__ P, uint32_t M, uint32_t N, uint32_t Kp, uint32_t spin_limit,
-                   unsigned int* err) {
+                   unsigned int* err, uint32_t tiles_n, uint32_t group_m) {
   using SH = Shape<BN_T>;
   constexpr int BN = SH::BN, BK = SH::BK;
   constexpr int STAGE_BYTES = PARTS * (SH::A_TILE + SH::B_TILE);
@@ -179,7 +187,15 @@ gemm_3xbf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;  // 1024-aligned stage ring
-  const uint32_t n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
+  uint32_t n0, m0;
+  {
+    const uint32_t tiles_m = gridDim.x / tiles_n, per_group = group_m * tiles_n;
+    const uint32_t grp = blockIdx.x / per_group, r = blockIdx.x % per_group;
+    const uint32_t first = grp * group_m;
+    const uint32_t rows = tiles_m - first < group_m ? tiles_m - first : group_m;
+    m0 = (first + r % rows) * BM;
+    n0 = (r / rows) * BN;
+  }
   const uint32_t nk = Kp / BK;
 
   if (threadIdx.x == 0) {
@@ -434,34 +450,30 @@ namespace {
 template <int PARTS, int STAGES, int G, int BN_T>
 cudaError_t launch_gemm(dim3 grid, cudaStream_t stream, const CUtensorMap& tmA, const CUtensorMap& tmB,
                         float* P, uint32_t M, uint32_t N, uint32_t Kp, uint32_t spin_limit,
-                        unsigned int* err) {
+                        unsigned int* err, uint32_t tiles_n, uint32_t group_m) {
   using SH = tc::Shape<BN_T>;
   const size_t smem = (size_t)STAGES * PARTS * (SH::A_TILE + SH::B_TILE) + 1024;
   auto kern = tc::gemm_3xbf16_kernel<PARTS, STAGES, G, BN_T>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kern<<<grid, SH::THREADS, smem, stream>>>(tmA, tmB, P, M, N, Kp, spin_limit, err);
+  kern<<<grid, SH::THREADS, smem, stream>>>(tmA, tmB, P, M, N, Kp, spin_limit, err, tiles_n, group_m);
   return cudaGetLastError();
 }
 }  // namespace
 
-int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uint32_t N,
-                       uint32_t K, int parts, int trans, int drain, int wide, void* scratch,
-                       size_t scratch_bytes, cudaStream_t stream, uint32_t spin_limit,
-                       unsigned int* err) {
-  if (parts != 2 && parts != 3) return fail(SCL_ERR_ARG, "3xBF16: parts must be 2 or 3");
+// The split pass: both operands into `parts` bf16 planes, K-major ([row][k]
+// and [col][k]), zero-padded to Mp / Np / Kp, in `scratch` (1024-aligned
+// inside it).  A transposed operand (trans bit 0: A stored K x M, bit 1: B
+// stored N x K) swaps which of the two split kernels produces it.
+void split_operands(const float* A, const float* B, uint32_t M, uint32_t N, uint32_t K, int parts,
+                    int trans, void* scratch, cudaStream_t stream, __nv_bfloat16** a_out,
+                    __nv_bfloat16** b_out) {
   const uint32_t Mp = tc::round_up(M, tc::BM), Np = tc::round_up(N, tc::NPAD),
                  Kp = tc::round_up(K, tc::KPAD);
-  if (scratch_bytes < allpairs_tc_scratch_bytes(M, N, K, parts))
-    return fail(SCL_ERR_ARG, "3xBF16: scratch too small");
   uint8_t* s = reinterpret_cast<uint8_t*>(((uintptr_t)scratch + 1023) & ~(uintptr_t)1023);
   __nv_bfloat16* a_parts = reinterpret_cast<__nv_bfloat16*>(s);
   __nv_bfloat16* b_parts = a_parts + (size_t)parts * Mp * Kp;
-
   const int sm = rt().sm_count > 0 ? rt().sm_count : 148;
-  // both operands end up K-major ([row][k] and [col][k]); a transposed
-  // operand (trans bit 0: A stored K x M, bit 1: B stored N x K) swaps which
-  // of the two split kernels produces it
   if (trans & 1) {
     dim3 agrid((Mp + 31) / 32, (Kp + 31) / 32);
     tc::split_transpose_kernel<<<agrid, dim3(32, 8), 0, stream>>>(A, K, M, Mp, Kp, parts, a_parts);
@@ -475,29 +487,52 @@ int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uin
     tc::split_transpose_kernel<<<tgrid, dim3(32, 8), 0, stream>>>(B, K, N, Np, Kp, parts, b_parts);
   }
   rt().launches += 2;
+  *a_out = a_parts;
+  *b_out = b_parts;
+}
+
+int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uint32_t N,
+                       uint32_t K, int parts, int trans, int drain, int wide, uint32_t group_rows,
+                       void* scratch, size_t scratch_bytes, cudaStream_t stream, uint32_t spin_limit,
+                       unsigned int* err) {
+  if (parts != 2 && parts != 3) return fail(SCL_ERR_ARG, "3xBF16: parts must be 2 or 3");
+  const uint32_t Mp = tc::round_up(M, tc::BM), Np = tc::round_up(N, tc::NPAD),
+                 Kp = tc::round_up(K, tc::KPAD);
+  if (scratch_bytes < allpairs_tc_scratch_bytes(M, N, K, parts))
+    return fail(SCL_ERR_ARG, "3xBF16: scratch too small");
+  __nv_bfloat16 *a_parts = nullptr, *b_parts = nullptr;
+  split_operands(A, B, M, N, K, parts, trans, scratch, stream, &a_parts, &b_parts);
 
   alignas(64) CUtensorMap tmA, tmB;
   const uint32_t bn = wide ? 256 : 128, bk = wide ? 32 : 64;
   if (int st = encode_parts(&tmA, a_parts, Mp, Kp, parts, tc::BM, bk)) return st;
   if (int st = encode_parts(&tmB, b_parts, Np, Kp, parts, bn, bk)) return st;
 
-  dim3 grid((N + bn - 1) / bn, Mp / tc::BM);
-  if (grid.y > 65535) return fail(SCL_ERR_ARG, "3xBF16: too many row tiles");
+  // one 1D grid over the output tiles, grouped by `group_m` tile rows; the
+  // default is a group whose rows of A and columns of B for one wave of one
+  // block per SM fit in L2 together
+  const uint64_t tiles_n = (N + bn - 1) / bn, tiles_m = Mp / tc::BM;
+  if (tiles_n * tiles_m > 0x7fffffffull) return fail(SCL_ERR_ARG, "3xBF16: too many output tiles");
+  uint32_t group_m = group_rows;
+  if (group_m == 0) group_m = 16;
+  if (group_m > tiles_m) group_m = (uint32_t)tiles_m;
+  dim3 grid((unsigned)(tiles_n * tiles_m));
+  const uint32_t tn = (uint32_t)tiles_n;
   cudaError_t e;
   if (wide) {
     // 128 x 256 tiles, k-blocks of 32: drains every 2 k-blocks (64 K, as the
     // narrow shape's default); parts 3: 3 stages of 72 KB; parts 2: 4 of 48 KB
-    e = parts == 3 ? launch_gemm<3, 3, 2, 256>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
-                   : launch_gemm<2, 4, 2, 256>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err);
+    e = parts == 3 ? launch_gemm<3, 3, 2, 256>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err, tn, group_m)
+                   : launch_gemm<2, 4, 2, 256>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err, tn, group_m);
   } else if (parts == 3) {
     // parts 3: 2 stages of 96 KB; parts 2: 3 stages of 64 KB
-    e = drain >= 4 ? launch_gemm<3, 2, 4, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
-      : drain == 2 ? launch_gemm<3, 2, 2, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
-                   : launch_gemm<3, 2, 1, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err);
+    e = drain >= 4 ? launch_gemm<3, 2, 4, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err, tn, group_m)
+      : drain == 2 ? launch_gemm<3, 2, 2, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err, tn, group_m)
+                   : launch_gemm<3, 2, 1, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err, tn, group_m);
   } else {
-    e = drain >= 4 ? launch_gemm<2, 3, 4, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
-      : drain == 2 ? launch_gemm<2, 3, 2, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err)
-                   : launch_gemm<2, 3, 1, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err);
+    e = drain >= 4 ? launch_gemm<2, 3, 4, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err, tn, group_m)
+      : drain == 2 ? launch_gemm<2, 3, 2, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err, tn, group_m)
+                   : launch_gemm<2, 3, 1, 128>(grid, stream, tmA, tmB, P, M, N, Kp, spin_limit, err, tn, group_m);
   }
   if (e != cudaSuccess) return cuda_fail(e, "3xBF16 launch");
   rt().launches += 1;
@@ -505,3 +540,20 @@ int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uin
 }
 
 }  // namespace scl
+
+using namespace scl;
+
+extern "C" int scl_debug_allpairs_split(const float* A, const float* B, uint32_t M, uint32_t N,
+                                        uint32_t K, int parts, int trans, void* scratch,
+                                        size_t scratch_bytes, size_t* needed) {
+  if (parts != 2 && parts != 3) return fail(SCL_ERR_ARG, "split: parts must be 2 or 3");
+  const size_t need = allpairs_tc_scratch_bytes(M, N, K, parts);
+  if (needed) *needed = need;
+  if (!scratch) return SCL_OK;
+  if (int st = require_init()) return st;
+  if (!A || !B || scratch_bytes < need) return fail(SCL_ERR_ARG, "split: null operand or scratch too small");
+  __nv_bfloat16 *a = nullptr, *b = nullptr;
+  split_operands(A, B, M, N, K, parts, trans, scratch, rt().stream, &a, &b);
+  SCL_CUDA(cudaGetLastError());
+  return SCL_OK;
+}

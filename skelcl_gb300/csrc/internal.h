@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <deque>
 #include <functional>
 #include <map>
 #include <memory>
@@ -112,6 +113,11 @@ struct Kernel {
 struct Workspace {  // per-program scratch (reduce partials, scan tile status)
   void* ptr = nullptr;
   size_t bytes = 0;
+  // A launch recorded into a CUDA graph keeps this allocation's address: when
+  // it must grow (or change layout) afterwards it is retired, not freed, so
+  // the graph stays valid; retired allocations are freed with the program.
+  bool recorded = false;
+  std::vector<void*> retired;
   // Scan status (scan.cuh): tiles per region, the allocation that layout
   // was cleared in, launches made since, and the slots the last launch in
   // each of the two alternating regions may have written
@@ -180,7 +186,10 @@ struct scl_program {
 
 namespace scl {
 CUfunction find_kernel(scl_program* p, const std::string& name);
-int ensure_workspace(scl_program* p, size_t bytes);
+// At least `bytes` of workspace (a new, zeroed allocation when it grows, or
+// when `fresh`).  Inside a stream capture it only notes that a graph now
+// uses the allocation; growing there is refused.
+int ensure_workspace(scl_program* p, size_t bytes, bool fresh = false);
 
 // Kernel parameters of one launch (launch.cpp)
 struct ArgPack {
@@ -211,6 +220,30 @@ size_t segments_prepare_scratch(uint64_t n_seg);
 int segments_prepare(const uint64_t* seg_offsets, uint64_t n_seg, uint64_t n_total, uint64_t tile,
                      uint64_t vg, uint64_t a, int reverse, uint64_t short_max, uint64_t* off_out,
                      unsigned int* tile_start, uint64_t* scratch, cudaStream_t stream);
+// Segment plans (segments.cu, scl_segplan_create): the clamped offsets of
+// one segmented vector, the segmented Reduce's per-segment tickets (zero
+// between launches: the last tile of a segment resets its ticket), and per
+// tile shape the tile numbering with its exact tile count.
+struct SegPlanCfg {
+  uint64_t tile = 0, vg = 1, a = 0, short_max = 0;
+  int reverse = 0;
+  unsigned int* tile_start = nullptr;  // device, n_seg + 1
+  uint64_t tiles = 0;                  // tile_start[n_seg]
+};
+struct SegPlan {
+  uint32_t id = 0;
+  uint64_t n_seg = 0, n_total = 0;
+  uint64_t* off = nullptr;
+  unsigned int* tickets = nullptr;
+  uint64_t* scratch = nullptr;
+  std::deque<SegPlanCfg> cfgs;  // (stable addresses)
+};
+SegPlan* segplan_find(uint32_t id);
+// The plan's tile numbering for one tile shape, built on first use (three
+// small launches and a read-back of the tile count; refused inside a stream
+// capture).
+int segplan_config(SegPlan* p, uint64_t tile, uint64_t vg, uint64_t a, int reverse, uint64_t short_max,
+                   const SegPlanCfg** out);
 // Autotuner (tune.cpp): lookup/store of the (device, program, skeleton, size
 // bucket) cache, and the launch wrapper that times `cands` on a miss.
 bool tune_lookup(const std::string& key, scl_tuning* out);

@@ -12,8 +12,8 @@
 // tcgen05 contraction (allpairs_tc.cu)
 namespace scl {
 int allpairs_tc_launch(const float* A, const float* B, float* P, uint32_t M, uint32_t N,
-                       uint32_t K, int parts, int trans, int drain, int wide, void* scratch,
-                       size_t scratch_bytes, cudaStream_t stream, uint32_t spin_limit,
+                       uint32_t K, int parts, int trans, int drain, int wide, uint32_t group_rows,
+                       void* scratch, size_t scratch_bytes, cudaStream_t stream, uint32_t spin_limit,
                        unsigned int* err);
 // row-major rows x cols -> cols x rows, elements of 4 or 8 bytes (adjoint.cu)
 int transpose_launch(const void* src, void* dst, uint64_t rows, uint64_t cols, size_t elem,
@@ -328,6 +328,57 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
   const size_t tsz = p->type_sizes[0], csz = p->carry_size ? p->carry_size : tsz;
   const int V = vec_width(tsz);
   int aligned = aligned16(in) ? 1 : 0;
+  if (sh->n_segments && sh->seg_plan) {
+    // a segment plan: one launch, tiles first, then a warp per short segment
+    SegPlan* pl = segplan_find(sh->seg_plan);
+    if (!pl) return fail(SCL_ERR_ARG, "segmented reduce: no segment plan " + std::to_string(sh->seg_plan));
+    if (pl->n_seg != sh->n_segments || pl->n_total > n)
+      return fail(SCL_ERR_ARG, "segmented reduce: the plan was made for other segments or a longer vector");
+    uint64_t n_seg = sh->n_segments;
+    const uint32_t R = (tu && tu->items == 8) ? 8 : 32;
+    const uint64_t tile = (uint64_t)R * 256 * V;
+    uint64_t short_max = kSegShort;
+    const SegPlanCfg* cfg = nullptr;
+    if (int st = segplan_config(pl, tile, 1, 0, 0, short_max, &cfg)) return st;
+    void* offs = pl->off;
+    unsigned int* err = rt().dev_err;
+    if (cfg->tiles == 0) {
+      // every vector short: the warp-per-vector kernel alone (no tile role,
+      // so no register cap from it and more blocks per SM)
+      CUfunction fs = find_kernel(p, "scl_reduce_short<8>");
+      if (!fs) return fail(SCL_ERR_LAUNCH, "kernel scl_reduce_short<8> missing");
+      ArgPack spack;
+      spack.ptrs = {&in, &out, &offs, &n_seg, &short_max};
+      if (int st = pack_extra(p, fs, spack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &spack))
+        return st;
+      uint64_t sb = (n_seg + 7) / 8;
+      const uint64_t smx = (uint64_t)max_resident_blocks(fs, 256, spack.local_bytes);
+      if (sb > smx) sb = smx;
+      p->last_variant = SCL_VARIANT_VECTOR;
+      return launch(fs, dim3((unsigned)std::max<uint64_t>(sb, 1)), dim3(256), 0, spack);
+    }
+    const std::string kname = "scl_reduce_seg<" + std::to_string(R) + ", 1>";
+    CUfunction fn = find_kernel(p, kname);
+    if (!fn) return fail(SCL_ERR_LAUNCH, "kernel " + kname + " missing");
+    // partials after the first 256 bytes: the flat reduce keeps its ticket
+    // there, and it must stay zero between launches
+    if (int st = ensure_workspace(p, 256 + cfg->tiles * csz)) return st;
+    void* partials = (char*)p->ws.ptr + 256;
+    void* tstart = cfg->tile_start;
+    void* tickets = pl->tickets;
+    ArgPack pack;
+    pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max};
+    if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
+      return st;
+    // warps for the short segments: one per segment, at most what stays resident
+    uint64_t sblocks = (n_seg + 7) / 8;
+    const uint64_t smax = (uint64_t)max_resident_blocks(fn, 256, pack.local_bytes);
+    if (sblocks > smax) sblocks = smax;
+    const uint64_t grid = cfg->tiles + std::max<uint64_t>(sblocks, 1);
+    if (grid > 0x7fffffffull) return fail(SCL_ERR_ARG, "segmented reduce: too many tiles");
+    p->last_variant = SCL_VARIANT_VECTOR;
+    return launch(fn, dim3((unsigned)grid), dim3(256), 0, pack);
+  }
   if (sh->n_segments) {
     // one result per segment, one launch (plus the offsets pre-pass)
     if (!sh->seg_offsets) return fail(SCL_ERR_ARG, "segmented reduce: null seg_offsets");
@@ -374,7 +425,7 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
     if (int st = launch(fn_short, dim3((unsigned)sblocks), dim3(256), 0, spack)) return st;
     // longer segments: tiles (blocks past the last tile return at once)
     ArgPack pack;
-    pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err};
+    pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max};
     if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
       return st;
     p->last_variant = SCL_VARIANT_VECTOR;
@@ -523,8 +574,15 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
     smem = 0;
   }
   uint64_t n_seg = sh->n_segments;
+  SegPlan* plan = nullptr;
+  if (n_seg && sh->seg_plan) {
+    plan = segplan_find(sh->seg_plan);
+    if (!plan) return fail(SCL_ERR_ARG, "segmented scan: no segment plan " + std::to_string(sh->seg_plan));
+    if (plan->n_seg != n_seg || plan->n_total > n)
+      return fail(SCL_ERR_ARG, "segmented scan: the plan was made for other segments or a longer vector");
+  }
   if (n_seg) {  // segmented: the staged kernel with the default tile shape
-    if (!sh->seg_offsets) return fail(SCL_ERR_ARG, "segmented scan: null seg_offsets");
+    if (!sh->seg_offsets && !plan) return fail(SCL_ERR_ARG, "segmented scan: null seg_offsets");
     staged = true;
     R = (tu && tu->items == 16) ? 16 : 8;
     smem = (size_t)R * 256 * V * tsz;
@@ -535,7 +593,29 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   uint64_t vg = 1, ga = 0;
   scan_grid(in, tsz, staged, &vg, &ga);
   uint64_t tiles;
-  if (n_seg) {
+  const SegPlanCfg* pcfg = nullptr;
+  if (plan) {
+    // the plan's exact count
+    if (int st = segplan_config(plan, tile, vg, ga, reverse ? 1 : 0, kSegShort, &pcfg)) return st;
+    tiles = pcfg->tiles;
+    if (tiles == 0) {
+      // every vector short: the warp-per-vector kernel alone (no tile role,
+      // so no register cap from it and more blocks per SM)
+      CUfunction fs = find_kernel(p, "scl_scan_short<8>");
+      if (!fs) return fail(SCL_ERR_LAUNCH, "kernel scl_scan_short<8> missing");
+      void* offs = plan->off;
+      uint64_t short_max = kSegShort;
+      ArgPack spack;
+      spack.ptrs = {&in, &out, &offs, &n_seg, &flags, &short_max};
+      if (int st = pack_extra(p, fs, spack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &spack))
+        return st;
+      uint64_t sb = (n_seg + 7) / 8;
+      const uint64_t smx = (uint64_t)max_resident_blocks(fs, 256, spack.local_bytes);
+      if (sb > smx) sb = smx;
+      p->last_variant = SCL_VARIANT_VECTOR;
+      return launch(fs, dim3((unsigned)std::max<uint64_t>(sb, 1)), dim3(256), 0, spack);
+    }
+  } else if (n_seg) {
     // an upper bound (the pre-pass has the count): tiles exist only for
     // segments longer than kSegShort, at most n / tile + 2 per such segment
     const uint64_t n_long = std::min<uint64_t>(n_seg, n / (kSegShort + 1) + 1);
@@ -556,18 +636,22 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   }
   if (n_seg) minb = R == 16 ? 3 : 6;
   const std::string kname = std::string(staged ? "scl_scan_s<" : "scl_scan_k<") + std::to_string(R) +
-                            ", " + std::to_string(minb) + (n_seg ? ", 1>" : ">");
+                            ", " + std::to_string(minb) + (plan ? ", 2>" : (n_seg ? ", 1>" : ">"));
   CUfunction fn = find_kernel(p, kname);
   if (!fn) return fail(SCL_ERR_LAUNCH, "kernel " + kname + " missing");
   // workspace: three status regions (scan_region_bytes); segmented launches
   // add [clamped offsets | tile numbering | pre-pass scratch] after them
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-  const size_t seg_of = n_seg ? up((n_seg + 1) * 8) : 0, seg_ts = n_seg ? up((n_seg + 1) * 4) : 0,
-               seg_sc = n_seg ? up(segments_prepare_scratch(n_seg)) : 0;
+  const bool prepass = n_seg && !plan;
+  const size_t seg_of = prepass ? up((n_seg + 1) * 8) : 0, seg_ts = prepass ? up((n_seg + 1) * 4) : 0,
+               seg_sc = prepass ? up(segments_prepare_scratch(n_seg)) : 0;
   Workspace& ws = p->ws;
   const uint64_t cap = std::max<uint64_t>({tiles, ws.scan_cap, 256});
   const size_t total = scan_status_bytes(p->status_mode, csz, cap);
-  if (int st = ensure_workspace(p, total + seg_of + seg_ts + seg_sc)) return st;
+  // a new status layout in an allocation a graph has recorded would move
+  // the graph's region under it: take a fresh allocation instead
+  const bool relayout = cap != ws.scan_cap || ws.scan_layout != ws.ptr;
+  if (int st = ensure_workspace(p, total + seg_of + seg_ts + seg_sc, relayout && ws.recorded)) return st;
   if (cap != ws.scan_cap || ws.scan_layout != ws.ptr) {
     SCL_CUDA(cudaMemsetAsync(ws.ptr, 0, total, rt().stream));
     ws.scan_cap = cap;
@@ -593,10 +677,20 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
     clr.flags = o.flags;
     clr.n = ws.scan_used[region ^ 1];
   }
-  void* seg_off = n_seg ? (char*)ws.ptr + total : nullptr;
-  void* tile_start = n_seg ? (char*)ws.ptr + total + seg_of : nullptr;
-  if (n_seg) {
-    uint64_t short_max = kSegShort;
+  void* seg_off = prepass ? (char*)ws.ptr + total : (plan ? (void*)plan->off : nullptr);
+  void* tile_start = prepass ? (char*)ws.ptr + total + seg_of : (plan ? (void*)pcfg->tile_start : nullptr);
+  uint64_t short_max = n_seg ? kSegShort : 0;
+  uint64_t grid = tiles;
+  if (plan) {
+    // the blocks past the tiles scan the short segments, a warp each
+    CUfunction f = find_kernel(p, kname);
+    uint64_t sblocks = (n_seg + 7) / 8;
+    const uint64_t smax = f ? (uint64_t)max_resident_blocks(f, 256, smem) : 1;
+    if (sblocks > smax) sblocks = smax;
+    grid = tiles + std::max<uint64_t>(sblocks, 1);
+    if (grid > 0x7fffffffull) return fail(SCL_ERR_ARG, "segmented scan: too many tiles");
+  }
+  if (prepass) {
     uint64_t* scratch = reinterpret_cast<uint64_t*>((char*)p->ws.ptr + total + seg_of + seg_ts);
     if (int st = segments_prepare(sh->seg_offsets, n_seg, n, tile, vg, ga, reverse ? 1 : 0, short_max,
                                   (uint64_t*)seg_off, (unsigned int*)tile_start, scratch, rt().stream))
@@ -622,11 +716,12 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
     pack.ptrs.push_back(&seg_off);
     pack.ptrs.push_back(&tile_start);
     pack.ptrs.push_back(&n_seg);
+    pack.ptrs.push_back(&short_max);
   }
   if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
     return st;
   p->last_variant = staged ? SCL_VARIANT_TMA : SCL_VARIANT_VECTOR;
-  if (int st = launch(fn, dim3((unsigned)tiles), dim3(256), smem, pack)) return st;
+  if (int st = launch(fn, dim3((unsigned)grid), dim3(256), smem, pack)) return st;
   if (!recorded) {  // this launch's region now holds up to `tiles` slots; the other is clean
     ws.scan_used[region] = tiles;
     ws.scan_used[region ^ 1] = 0;
@@ -738,9 +833,11 @@ extern "C" int scl_launch_allpairs(scl_program* p, const scl_shape* sh, void* co
       const uint64_t wide_tiles = (uint64_t)((M + 127u) / 128u) * ((N + 255u) / 256u);
       const uint64_t sms = rt().sm_count > 0 ? (uint64_t)rt().sm_count : 148u;
       const int wide = cols == 256u || (cols == 0u && wide_tiles >= sms) ? 1 : 0;
+      // tuning.workgroup: output-tile rows per group of the tile order (0: 16)
+      const uint32_t group_rows = tu ? tu->workgroup : 0u;
       return allpairs_tc_launch((const float*)A, (const float*)B, (float*)P, M, N, K, parts, trans,
-                                drain, wide, p->ws.ptr, p->ws.bytes, rt().stream, spin_of(tu),
-                                rt().dev_err);
+                                drain, wide, group_rows, p->ws.ptr, p->ws.bytes, rt().stream,
+                                spin_of(tu), rt().dev_err);
     }
     if (want == SCL_VARIANT_TC3XBF16)
       return fail(SCL_ERR_UNSUPPORTED, "the tensor-core AllPairs needs zip x*y, reduce x+y, identity 0, "

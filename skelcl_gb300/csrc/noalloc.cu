@@ -147,13 +147,14 @@ extern "C" int scl_launch_scan_noalloc(scl_program* p, const scl_shape* sh, void
   unsigned int* err = rt().dev_err;
   const void* seg_off = nullptr;
   const void* tile_start = nullptr;
-  uint64_t n_seg = 0;
+  uint64_t n_seg = 0, short_max = 0;
   ArgPack pack;
   pack.ptrs = {&in, &out, &n, &fl, &aligned, &ticket, &sargs, &clr, &spin, &err};
   if (staged) {
     pack.ptrs.push_back(&seg_off);
     pack.ptrs.push_back(&tile_start);
     pack.ptrs.push_back(&n_seg);
+    pack.ptrs.push_back(&short_max);
   }
   if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
     return st;

@@ -342,6 +342,7 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
       s << scl_tpl_reduce;
       out->kernels = {"scl_reduce_k<8>", "scl_reduce_k<4>"};
       out->lazy = {"scl_reduce_k<1>", "scl_reduce_k<2>", "scl_reduce_seg<32>", "scl_reduce_seg<8>",
+                   "scl_reduce_seg<32, 1>", "scl_reduce_seg<8, 1>",
                    "scl_reduce_short<8>"};
       break;
     case SCL_KIND_SCAN:
@@ -351,7 +352,7 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
                    "scl_scan_k<2, 8>", "scl_scan_k<16, 2>", "scl_scan_k<16, 1>",
                    "scl_scan_s<8, 5>", "scl_scan_s<8, 4>", "scl_scan_s<4, 8>", "scl_scan_s<6, 8>",
                    "scl_scan_s<16, 3>", "scl_scan_s<8, 6, 1>", "scl_scan_s<16, 3, 1>",
-                   "scl_scan_short<8>"};
+                   "scl_scan_s<8, 6, 2>", "scl_scan_s<16, 3, 2>", "scl_scan_short<8>"};
       break;
     case SCL_KIND_ZIP_REDUCE:
       s << scl_tpl_reduce;
@@ -361,8 +362,8 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
       s << scl_tpl_reduce << "\n" << scl_tpl_scan;
       out->kernels = {"scl_scan_s<8, 6>"};
       out->lazy = {"scl_scan_s<8, 5>", "scl_scan_s<8, 4>", "scl_scan_s<4, 8>", "scl_scan_s<6, 8>",
-                   "scl_scan_s<16, 3>",
-                   "scl_scan_s<8, 6, 1>", "scl_scan_s<16, 3, 1>", "scl_scan_short<8>"};
+                   "scl_scan_s<16, 3>", "scl_scan_s<8, 6, 1>", "scl_scan_s<16, 3, 1>",
+                   "scl_scan_s<8, 6, 2>", "scl_scan_s<16, 3, 2>", "scl_scan_short<8>"};
       break;
     case SCL_KIND_MAPOVERLAP:
       s << scl_tpl_mapoverlap;
@@ -635,13 +636,24 @@ CUfunction find_kernel(scl_program* p, const std::string& name) {
   return it == p->kernels.end() ? nullptr : it->second.fn;
 }
 
-int ensure_workspace(scl_program* p, size_t bytes) {
-  if (p->ws.bytes >= bytes) return SCL_OK;
+int ensure_workspace(scl_program* p, size_t bytes, bool fresh) {
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  SCL_CUDA(cudaStreamIsCapturing(rt().stream, &capture));
+  const bool capturing = capture != cudaStreamCaptureStatusNone;
+  if (p->ws.bytes >= bytes && !fresh) {
+    if (capturing) p->ws.recorded = true;
+    return SCL_OK;
+  }
+  if (capturing)
+    return fail(SCL_ERR_ARG, "the program's workspace would grow inside a stream capture; make the "
+                             "same call once before capturing");
   if (p->ws.ptr) {
     cudaStreamSynchronize(rt().stream);
-    cudaFree(p->ws.ptr);
+    if (p->ws.recorded) p->ws.retired.push_back(p->ws.ptr);  // a graph may still use it
+    else cudaFree(p->ws.ptr);
     p->ws.ptr = nullptr;
     p->ws.bytes = 0;
+    p->ws.recorded = false;
   }
   size_t sz = bytes < 4096 ? 4096 : bytes;
   cudaError_t e = cudaMalloc(&p->ws.ptr, sz);
@@ -814,6 +826,7 @@ extern "C" int scl_program_release(scl_program* p) {
   if (rt().initialized) {
     cudaStreamSynchronize(rt().stream);
     if (p->ws.ptr) cudaFree(p->ws.ptr);
+    for (void* r : p->ws.retired) cudaFree(r);
     for (CUmodule m : p->modules) rt().drv.cuModuleUnload(m);
   }
   delete p;

@@ -17,6 +17,9 @@
 // them in a separate kernel.  tile_start[n_segments] is the tile count.
 #include <cstdint>
 #include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
 
 #include "internal.h"
 
@@ -77,7 +80,8 @@ __device__ __forceinline__ uint64_t seg_tiles(uint64_t lo, uint64_t hi, uint64_t
   return (len + m + tile - 1) / tile;
 }
 
-// 1. clamp the offsets, count each segment's tiles, one sum per block
+// 1. clamp the offsets (written to off_out unless it is null), count each
+//    segment's tiles, one sum per block
 __global__ void __launch_bounds__(kSegThreads)
 seg_clamp_count_kernel(const uint64_t* off_in, uint64_t n_seg, uint64_t n_total, uint64_t tile,
                        uint64_t vg, uint64_t a, int reverse, uint64_t short_max, uint64_t* off_out,
@@ -95,9 +99,9 @@ seg_clamp_count_kernel(const uint64_t* off_in, uint64_t n_seg, uint64_t n_total,
     const uint64_t lo = rlo < n_total ? rlo : n_total;
     uint64_t hi = rhi < n_total ? rhi : n_total;
     if (hi < lo) hi = lo;
-    off_out[sg] = lo;
+    if (off_out) off_out[sg] = lo;
     if (sg + 1 == n_seg) {
-      off_out[n_seg] = rhi < n_total ? rhi : n_total;
+      if (off_out) off_out[n_seg] = rhi < n_total ? rhi : n_total;
       bad = bad || rhi > n_total;
     }
     sum += seg_tiles(lo, hi, tile, vg, a, reverse, short_max);
@@ -229,8 +233,11 @@ int segments_prepare(const uint64_t* seg_offsets, uint64_t n_seg, uint64_t n_tot
   const uint64_t nb = (n_seg + kSegPerBlock - 1) / kSegPerBlock;
   if (nb == 0) return SCL_OK;
   if (nb > 0x7fffffffull) return fail(SCL_ERR_ARG, "too many segments");
+  // off_out == seg_offsets: the offsets are already clamped; number the
+  // tiles without writing them again
   seg_clamp_count_kernel<<<(unsigned)nb, kSegThreads, 0, stream>>>(
-      seg_offsets, n_seg, n_total, tile, vg, a, reverse, short_max, off_out, scratch, rt().dev_err);
+      seg_offsets, n_seg, n_total, tile, vg, a, reverse, short_max,
+      off_out == seg_offsets ? nullptr : off_out, scratch, rt().dev_err);
   seg_scan_sums_kernel<<<1, kPrepThreads, 0, stream>>>(scratch, nb);
   seg_tile_start_kernel<<<(unsigned)nb, kSegThreads, 0, stream>>>(off_out, n_seg, tile, vg, a, reverse,
                                                                   short_max, scratch, nb, tile_start);
@@ -239,9 +246,118 @@ int segments_prepare(const uint64_t* seg_offsets, uint64_t n_seg, uint64_t n_tot
   return SCL_OK;
 }
 
+// ---- segment plans ------------------------------------------------------------
+namespace {
+std::mutex g_plan_mu;
+std::map<uint32_t, std::unique_ptr<SegPlan>> g_plans;
+uint32_t g_next_plan = 1;
+
+void free_plan(SegPlan* p) {
+  if (!rt().initialized) return;
+  cudaStreamSynchronize(rt().stream);
+  cudaFree(p->off);
+  cudaFree(p->tickets);
+  cudaFree(p->scratch);
+  for (auto& c : p->cfgs) cudaFree(c.tile_start);
+}
+}  // namespace
+
+SegPlan* segplan_find(uint32_t id) {
+  std::lock_guard<std::mutex> g(g_plan_mu);
+  auto it = g_plans.find(id);
+  return it == g_plans.end() ? nullptr : it->second.get();
+}
+
+int segplan_config(SegPlan* p, uint64_t tile, uint64_t vg, uint64_t a, int reverse, uint64_t short_max,
+                   const SegPlanCfg** out) {
+  for (auto& c : p->cfgs)
+    if (c.tile == tile && c.vg == vg && c.a == a && c.reverse == reverse && c.short_max == short_max) {
+      *out = &c;
+      return SCL_OK;
+    }
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  SCL_CUDA(cudaStreamIsCapturing(rt().stream, &capture));
+  if (capture != cudaStreamCaptureStatusNone)
+    return fail(SCL_ERR_ARG,
+                "segment plan: this tile shape is first used inside a stream capture; make the call "
+                "once before capturing (building its tile numbering reads the tile count back)");
+  SegPlanCfg c;
+  c.tile = tile;
+  c.vg = vg;
+  c.a = a;
+  c.reverse = reverse;
+  c.short_max = short_max;
+  rt().device_allocs++;
+  SCL_CUDA(cudaMalloc(&c.tile_start, (p->n_seg + 1) * sizeof(unsigned int)));
+  if (int st = segments_prepare(p->off, p->n_seg, p->n_total, tile, vg, a, reverse, short_max, p->off,
+                                c.tile_start, p->scratch, rt().stream)) {
+    cudaFree(c.tile_start);
+    return st;
+  }
+  unsigned int tiles = 0;
+  SCL_CUDA(cudaMemcpyAsync(&tiles, c.tile_start + p->n_seg, sizeof(tiles), cudaMemcpyDeviceToHost,
+                           rt().stream));
+  SCL_CUDA(cudaStreamSynchronize(rt().stream));
+  c.tiles = tiles;
+  p->cfgs.push_back(c);
+  *out = &p->cfgs.back();
+  return SCL_OK;
+}
+
 }  // namespace scl
 
 using namespace scl;
+
+extern "C" int scl_segplan_create(const uint64_t* seg_offsets, uint64_t n_segments, uint64_t n,
+                                  uint32_t* plan) {
+  if (int st = require_init()) return st;
+  if (!plan) return fail(SCL_ERR_ARG, "scl_segplan_create: null plan");
+  *plan = 0;
+  if (!seg_offsets || n_segments == 0) return fail(SCL_ERR_ARG, "scl_segplan_create: no segments");
+  const uint64_t nb = (n_segments + kSegPerBlock - 1) / kSegPerBlock;
+  if (nb > 0x7fffffffull) return fail(SCL_ERR_ARG, "scl_segplan_create: too many segments");
+  std::unique_ptr<SegPlan> p(new SegPlan);
+  p->n_seg = n_segments;
+  p->n_total = n;
+  rt().device_allocs += 3;
+  cudaError_t e = cudaMalloc(&p->off, (n_segments + 1) * sizeof(uint64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&p->tickets, n_segments * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc(&p->scratch, segments_prepare_scratch(n_segments));
+  if (e == cudaSuccess) e = cudaMemsetAsync(p->tickets, 0, n_segments * sizeof(unsigned int), rt().stream);
+  if (e != cudaSuccess) {
+    free_plan(p.get());
+    cudaGetLastError();
+    return fail(SCL_ERR_OOM, "scl_segplan_create: device memory for the plan");
+  }
+  // the clamped copy of the offsets (no tiles counted yet)
+  seg_clamp_count_kernel<<<(unsigned)nb, kSegThreads, 0, rt().stream>>>(
+      seg_offsets, n_segments, n, ~0ull, 1, 0, 0, ~0ull, p->off, p->scratch, rt().dev_err);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    free_plan(p.get());
+    return cuda_fail(e, "segment plan: clamp kernel");
+  }
+  ++rt().launches;
+  std::lock_guard<std::mutex> g(g_plan_mu);
+  p->id = g_next_plan++;
+  if (g_next_plan == 0) g_next_plan = 1;
+  *plan = p->id;
+  g_plans[p->id] = std::move(p);
+  return SCL_OK;
+}
+
+extern "C" int scl_segplan_release(uint32_t plan) {
+  std::unique_ptr<SegPlan> p;
+  {
+    std::lock_guard<std::mutex> g(g_plan_mu);
+    auto it = g_plans.find(plan);
+    if (it == g_plans.end()) return plan == 0 ? SCL_OK : fail(SCL_ERR_ARG, "scl_segplan_release: no such plan");
+    p = std::move(it->second);
+    g_plans.erase(it);
+  }
+  free_plan(p.get());
+  return SCL_OK;
+}
 
 extern "C" int scl_adjoint_broadcast_segments(const void* g, void* gx, const uint64_t* seg_offsets,
                                               uint64_t n_segments, uint64_t n, int dtype,

@@ -199,6 +199,70 @@ __global__ void scl_reduce_k(const scl_T* in, scl_T* out, scl_u64 n, int aligned
   }
 }
 
+// Segments of at most short_max elements (empty ones included: SCL_IDENTITY):
+// one warp each, warps striding over the segments (warp `wid` of `nw`), U
+// elements per lane in flight, folded in the element type (no block boundary
+// is crossed; FP64 folds here would make the FP64 pipe the bound for tiny
+// segments); longer segments are left to the tiles.
+template <int U>
+__device__ __forceinline__ void scl_reduce_short_run(const scl_T* in, scl_T* out, const scl_u64* seg_off,
+                                                     scl_u64 n_seg, scl_u64 short_max, scl_u64 wid,
+                                                     scl_u64 nw SCL_USER_PARAMS) {
+  const int lane = threadIdx.x & 31;
+  scl_u64 sg = wid;
+  // the next segment's offsets are loaded while this one is folded
+  scl_u64 lo_next = sg < n_seg ? seg_off[sg] : 0, hi_next = sg < n_seg ? seg_off[sg + 1] : 0;
+  for (; sg < n_seg; sg += nw) {
+    const scl_u64 lo = lo_next;
+    const scl_u64 len = hi_next > lo ? hi_next - lo : 0;
+    if (sg + nw < n_seg) {
+      lo_next = seg_off[sg + nw];
+      hi_next = seg_off[sg + nw + 1];
+    }
+    if (len > short_max) continue;
+    bool have = false;
+    scl_T acc;
+    for (scl_u64 b = 0; b < len; b += 32 * U) {
+      scl_T v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const scl_u64 e = b + (scl_u64)(u * 32 + lane);
+        if (e < len) v[u] = in[lo + e];
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (b + (scl_u64)(u * 32 + lane) < len) {
+          acc = have ? SCL_FUNC(acc, v[u] SCL_OP_ARGS) : v[u];
+          have = true;
+        }
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const scl_T o = scl_shfl_down(acc, off);
+      const bool oh = __shfl_down_sync(0xffffffffu, have ? 1 : 0, off) != 0;
+      if (lane + off < 32 && oh) {
+        acc = have ? SCL_FUNC(acc, o SCL_OP_ARGS) : o;
+        have = true;
+      }
+    }
+    if (lane == 0) out[sg] = have ? acc : (scl_T)(SCL_IDENTITY);
+  }
+}
+
+// The warp-per-segment kernel on its own (segmented launches without a
+// segment plan; with one, scl_reduce_seg<R, 1> runs the same code in the
+// blocks past the tiles).
+template <int U>
+__global__ void __launch_bounds__(256)
+scl_reduce_short(const scl_T* in, scl_T* out, const scl_u64* seg_off, scl_u64 n_seg,
+                 scl_u64 short_max SCL_EXTRA_PARAMS) {
+  SCL_EXTRA_SETUP
+  scl_reduce_short_run<U>(in, out, seg_off, n_seg, short_max,
+                          ((scl_u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                          ((scl_u64)gridDim.x * blockDim.x) >> 5 SCL_EXTRA_ARGS);
+}
+
 // Segmented Reduce (no counterpart in the reference): out[s] = the fold of
 // segment [seg_off[s], seg_off[s+1]) of the flat vector, for every segment,
 // in one launch.  Tiles of R x 256 vectors never span segments (segment s
@@ -206,13 +270,25 @@ __global__ void scl_reduce_k(const scl_T* in, scl_T* out, scl_u64 n, int aligned
 // folds its elements into partials[tile], and the last tile of a segment to
 // finish (per-segment ticket, reset afterwards) folds that segment's
 // partials.  An empty segment yields SCL_IDENTITY.  Blocks past the last
-// tile (the grid is an upper bound) return at once.
-template <int R>
+// tile (the grid is an upper bound) return at once; with MERGED they fold
+// the segments of at most short_max elements instead, a warp each
+// (scl_reduce_short_run): one launch for a whole segmented Reduce.
+template <int R, int MERGED = 0>
 __global__ void __launch_bounds__(256)
 scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
                const unsigned int* tile_start, scl_u64 n_seg, int aligned, scl_C* partials,
-               unsigned int* tickets, unsigned int* err SCL_EXTRA_PARAMS) {
+               unsigned int* tickets, unsigned int* err, scl_u64 short_max SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
+  (void)short_max;
+  if constexpr (MERGED != 0) {
+    const unsigned int nt = tile_start[n_seg];
+    if (blockIdx.x >= nt) {
+      scl_reduce_short_run<8>(in, out, seg_off, n_seg, short_max,
+                              ((scl_u64)(blockIdx.x - nt) * 256 + threadIdx.x) >> 5,
+                              ((scl_u64)(gridDim.x - nt) * 256) >> 5 SCL_EXTRA_ARGS);
+      return;
+    }
+  }
   constexpr int V = scl_vec_width<sizeof(scl_T)>::value;
   constexpr int B = 256;
   constexpr scl_u64 TILE = (scl_u64)R * B * V;
@@ -317,58 +393,6 @@ scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
   }
 }
 
-// Segments of at most short_max elements (empty ones included: SCL_IDENTITY):
-// one warp each, grid-stride over the segments, U elements per lane in
-// flight, folded in the element type (no block boundary is crossed; FP64
-// folds here would make the FP64 pipe the bound for tiny segments); longer
-// segments are left to scl_reduce_seg.
-template <int U>
-__global__ void __launch_bounds__(256)
-scl_reduce_short(const scl_T* in, scl_T* out, const scl_u64* seg_off, scl_u64 n_seg,
-                 scl_u64 short_max SCL_EXTRA_PARAMS) {
-  SCL_EXTRA_SETUP
-  const int lane = threadIdx.x & 31;
-  const scl_u64 nw = ((scl_u64)gridDim.x * blockDim.x) >> 5;
-  scl_u64 sg = ((scl_u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  // the next segment's offsets are loaded while this one is folded
-  scl_u64 lo_next = sg < n_seg ? seg_off[sg] : 0, hi_next = sg < n_seg ? seg_off[sg + 1] : 0;
-  for (; sg < n_seg; sg += nw) {
-    const scl_u64 lo = lo_next;
-    const scl_u64 len = hi_next > lo ? hi_next - lo : 0;
-    if (sg + nw < n_seg) {
-      lo_next = seg_off[sg + nw];
-      hi_next = seg_off[sg + nw + 1];
-    }
-    if (len > short_max) continue;
-    bool have = false;
-    scl_T acc;
-    for (scl_u64 b = 0; b < len; b += 32 * U) {
-      scl_T v[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const scl_u64 e = b + (scl_u64)(u * 32 + lane);
-        if (e < len) v[u] = in[lo + e];
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        if (b + (scl_u64)(u * 32 + lane) < len) {
-          acc = have ? SCL_FUNC(acc, v[u] SCL_OP_ARGS) : v[u];
-          have = true;
-        }
-      }
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const scl_T o = scl_shfl_down(acc, off);
-      const bool oh = __shfl_down_sync(0xffffffffu, have ? 1 : 0, off) != 0;
-      if (lane + off < 32 && oh) {
-        acc = have ? SCL_FUNC(acc, o SCL_OP_ARGS) : o;
-        have = true;
-      }
-    }
-    if (lane == 0) out[sg] = have ? acc : (scl_T)(SCL_IDENTITY);
-  }
-}
 #endif  // SCL_KIND == 9
 
 #if SCL_KIND == 16

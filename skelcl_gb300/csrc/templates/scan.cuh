@@ -198,6 +198,7 @@ __device__ __forceinline__ scl_C scl_lookback(const scl_scan_status& st, long lo
   const scl_C cid = (scl_C)(scl_T)(SCL_IDENTITY);
   scl_C running = cid;  // fold of the tiles already visited (later ones)
   long long pred = tile - 1;
+  bool first_round = true;
   while (true) {
     const long long idx = pred - lane;
     scl_C v = cid;
@@ -214,7 +215,10 @@ __device__ __forceinline__ scl_C scl_lookback(const scl_scan_status& st, long lo
     // the usual case: the nearest predecessor already holds its inclusive
     // prefix, and nothing needs folding (the fold below costs five shuffle
     // rounds, in FP64 for float carries)
-    if (pmask & 1u) return (scl_C)SCL_FUNC_C(scl_shfl_idx(v, 0), running SCL_OP_ARGS);
+    if (pmask & 1u) {
+      const scl_C w = scl_shfl_idx(v, 0);
+      return first_round ? w : (scl_C)SCL_FUNC_C(w, running SCL_OP_ARGS);
+    }
     const int first_inc = pmask ? __ffs(pmask) - 1 : 31;  // nearest inclusive prefix
     if (lane > first_inc) v = cid;
     // ordered fold over lanes: higher lane = earlier tile
@@ -227,6 +231,7 @@ __device__ __forceinline__ scl_C scl_lookback(const scl_scan_status& st, long lo
     running = (scl_C)SCL_FUNC_C(window, running SCL_OP_ARGS);
     if (pmask) return running;
     pred -= 32;
+    first_round = false;
   }
 }
 
@@ -383,6 +388,101 @@ __device__ __forceinline__ bool scl_mbar_wait(unsigned int bar_s, unsigned int s
   return true;
 }
 
+// Segmented scan of the segments of at most short_max elements: one warp per
+// segment, warps striding over the segments (warp `wid` of `nw`); per round
+// each lane scans U contiguous elements serially, a warp scan combines the
+// lanes' totals, and rounds are chained through a carry in the element type
+// (no block boundary is crossed, as inside one tile of the tiled kernel; FP64
+// carries here would make the FP64 pipe the bound for tiny segments); longer
+// segments (and empty ones, which have nothing to write) are left to the
+// tiles.  Operand order and identity handling are those of the tiled kernel:
+// f(earlier, later), the exclusive form starts from SCL_IDENTITY.
+template <int U>
+__device__ __forceinline__ void scl_scan_short_run(const scl_T* in, scl_O* out, const scl_u64* seg_off,
+                                                   scl_u64 n_seg, unsigned int flags, scl_u64 short_max,
+                                                   scl_u64 wid, scl_u64 nw SCL_USER_PARAMS) {
+  const int lane = threadIdx.x & 31;
+  const bool inclusive = (flags & 1u) != 0, reverse = (flags & 2u) != 0;
+  const scl_T ident = (scl_T)(SCL_IDENTITY);
+  // round b of a segment [lo, hi): lane l holds the logical elements
+  // b + l*U .. b + l*U + U-1, which sit at lo + e, or at hi - 1 - e reversed
+  // (identity past the end, and nothing loaded for segments left to tiles)
+  auto load = [&](scl_T (&v)[U], scl_u64 lo, scl_u64 hi, scl_u64 b) {
+    const scl_u64 len = hi - lo;
+    const bool mine = len <= short_max;
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      const scl_u64 e = b + (scl_u64)lane * U + k;
+      v[k] = (mine && e < len) ? in[reverse ? hi - 1 - e : lo + e] : ident;
+    }
+  };
+  auto bounds = [&](scl_u64 sg, scl_u64* lo, scl_u64* hi) {
+    *lo = 0;
+    *hi = 0;
+    if (sg < n_seg) {
+      *lo = seg_off[sg];
+      const scl_u64 h = seg_off[sg + 1];
+      *hi = h > *lo ? h : *lo;
+    }
+  };
+  // software pipeline: the next segment's first round and the offsets of
+  // the one after are loaded while this segment is scanned
+  scl_u64 sg = wid;
+  scl_u64 lo, hi, lo_n, hi_n;
+  bounds(sg, &lo, &hi);
+  bounds(sg + nw, &lo_n, &hi_n);
+  scl_T v[U];
+  load(v, lo, hi, 0);
+  for (; sg < n_seg; sg += nw) {
+    scl_u64 lo_nn, hi_nn;
+    bounds(sg + 2 * nw, &lo_nn, &hi_nn);
+    scl_T vn[U];
+    load(vn, lo_n, hi_n, 0);
+    const scl_u64 len = hi - lo;
+    if (len > 0 && len <= short_max) {
+      scl_T carry = ident;
+      for (scl_u64 b = 0; b < len; b += 32 * U) {
+        if (b > 0) load(v, lo, hi, b);
+        const scl_u64 e0 = b + (scl_u64)lane * U;
+#pragma unroll
+        for (int k = 1; k < U; ++k) v[k] = SCL_FUNC(v[k - 1], v[k] SCL_OP_ARGS);
+        const scl_T tot = scl_warp_incl(v[U - 1] SCL_EXTRA_ARGS);
+        scl_T lane_excl = scl_shfl_up(tot, 1);
+        if (lane == 0) lane_excl = ident;
+        const scl_T pre = SCL_FUNC(carry, lane_excl SCL_OP_ARGS);
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+          const scl_u64 e = e0 + k;
+          if (e < len) {
+            const scl_T r = inclusive ? SCL_FUNC(pre, v[k] SCL_OP_ARGS)
+                                      : (k == 0 ? pre : SCL_FUNC(pre, v[k - 1] SCL_OP_ARGS));
+            out[reverse ? hi - 1 - e : lo + e] = SCL_EPILOGUE(r);
+          }
+        }
+        carry = SCL_FUNC(carry, scl_shfl_idx(tot, 31) SCL_OP_ARGS);
+      }
+    }
+    lo = lo_n;
+    hi = hi_n;
+    lo_n = lo_nn;
+    hi_n = hi_nn;
+#pragma unroll
+    for (int k = 0; k < U; ++k) v[k] = vn[k];
+  }
+}
+
+// The warp-per-segment kernel on its own (segmented launches without a
+// segment plan; with one, scl_scan_s<R, MINB, 2> runs the same code in the
+// blocks past the tiles).
+template <int U>
+__global__ void __launch_bounds__(256)
+scl_scan_short(const scl_T* in, scl_O* out, const scl_u64* seg_off, scl_u64 n_seg,
+               unsigned int flags, scl_u64 short_max SCL_EXTRA_PARAMS) {
+  SCL_EXTRA_SETUP
+  scl_scan_short_run<U>(in, out, seg_off, n_seg, flags, short_max,
+                        ((scl_u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                        ((scl_u64)gridDim.x * blockDim.x) >> 5 SCL_EXTRA_ARGS);
+}
 //
 // Tiles lie on the 16-byte grid of `in`: with `a` the first element index on
 // a 16-byte boundary, a (forward) sequence [lo, hi) starts its first tile at
@@ -400,14 +500,18 @@ __device__ __forceinline__ bool scl_mbar_wait(unsigned int bar_s, unsigned int s
 // tile_start[s] .. tile_start[s+1]-1 (at least one), and the look-back stops
 // at the segment's first tile.  Tickets past the last tile (the grid is an
 // upper bound) return at once.
+// SEG = 2: the same, and the blocks past the tiles scan the segments of at
+// most short_max elements, a warp each (scl_scan_short_run): one launch for
+// a whole segmented scan.
 template <int R, int MINB, int SEG = 0>
 __global__ void __launch_bounds__(SCL_SCAN_B, MINB)
 scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int aligned,
            unsigned int* tile_counter, scl_scan_status st, scl_scan_clear clr, unsigned int spin_limit,
            unsigned int* err, const scl_u64* seg_off, const unsigned int* tile_start,
-           scl_u64 n_seg SCL_EXTRA_PARAMS) {
+           scl_u64 n_seg, scl_u64 short_max SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
   (void)aligned;
+  (void)short_max;
   constexpr int B = SCL_SCAN_B, W = SCL_SCAN_W;
   constexpr int V = scl_vec_width<sizeof(scl_T)>::value;
   constexpr int TILE = R * B * V;
@@ -435,6 +539,15 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   scl_scan_clear_other(clr);
+  if constexpr (SEG == 2) {
+    const unsigned int nt = tile_start[n_seg];
+    if (blockIdx.x >= nt) {  // (block-uniform: no barrier below is reached)
+      scl_scan_short_run<4>(in, out, seg_off, n_seg, flags, short_max,
+                            ((scl_u64)(blockIdx.x - nt) * SCL_SCAN_B + threadIdx.x) >> 5,
+                            ((scl_u64)(gridDim.x - nt) * SCL_SCAN_B) >> 5 SCL_EXTRA_ARGS);
+      return;
+    }
+  }
   __syncthreads();
   const unsigned int tile = s_tile;
   unsigned int first = 0;  // ticket of the first tile of this tile's sequence
@@ -659,88 +772,4 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
   }
 }
 
-// Segmented scan of the segments of at most short_max elements: one warp per
-// segment, grid-stride over the segments; per round each lane scans U
-// contiguous elements serially, a warp scan combines the lanes' totals, and
-// rounds are chained through a carry in the element type (no block boundary is crossed, as inside one
-// tile of the tiled kernel; FP64 carries here would make the FP64 pipe the
-// bound for tiny segments); longer segments (and empty ones, which have
-// nothing to write) are left to scl_scan_s<R, MINB, 1>.  Operand order and
-// identity handling are those of the tiled kernel: f(earlier, later), the
-// exclusive form starts from SCL_IDENTITY.
-template <int U>
-__global__ void __launch_bounds__(256)
-scl_scan_short(const scl_T* in, scl_O* out, const scl_u64* seg_off, scl_u64 n_seg,
-               unsigned int flags, scl_u64 short_max SCL_EXTRA_PARAMS) {
-  SCL_EXTRA_SETUP
-  const int lane = threadIdx.x & 31;
-  const bool inclusive = (flags & 1u) != 0, reverse = (flags & 2u) != 0;
-  const scl_T ident = (scl_T)(SCL_IDENTITY);
-  const scl_u64 nw = ((scl_u64)gridDim.x * blockDim.x) >> 5;
-  // round b of a segment [lo, hi): lane l holds the logical elements
-  // b + l*U .. b + l*U + U-1, which sit at lo + e, or at hi - 1 - e reversed
-  // (identity past the end, and nothing loaded for segments left to tiles)
-  auto load = [&](scl_T (&v)[U], scl_u64 lo, scl_u64 hi, scl_u64 b) {
-    const scl_u64 len = hi - lo;
-    const bool mine = len <= short_max;
-#pragma unroll
-    for (int k = 0; k < U; ++k) {
-      const scl_u64 e = b + (scl_u64)lane * U + k;
-      v[k] = (mine && e < len) ? in[reverse ? hi - 1 - e : lo + e] : ident;
-    }
-  };
-  auto bounds = [&](scl_u64 sg, scl_u64* lo, scl_u64* hi) {
-    *lo = 0;
-    *hi = 0;
-    if (sg < n_seg) {
-      *lo = seg_off[sg];
-      const scl_u64 h = seg_off[sg + 1];
-      *hi = h > *lo ? h : *lo;
-    }
-  };
-  // software pipeline: the next segment's first round and the offsets of
-  // the one after are loaded while this segment is scanned
-  scl_u64 sg = ((scl_u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  scl_u64 lo, hi, lo_n, hi_n;
-  bounds(sg, &lo, &hi);
-  bounds(sg + nw, &lo_n, &hi_n);
-  scl_T v[U];
-  load(v, lo, hi, 0);
-  for (; sg < n_seg; sg += nw) {
-    scl_u64 lo_nn, hi_nn;
-    bounds(sg + 2 * nw, &lo_nn, &hi_nn);
-    scl_T vn[U];
-    load(vn, lo_n, hi_n, 0);
-    const scl_u64 len = hi - lo;
-    if (len > 0 && len <= short_max) {
-      scl_T carry = ident;
-      for (scl_u64 b = 0; b < len; b += 32 * U) {
-        if (b > 0) load(v, lo, hi, b);
-        const scl_u64 e0 = b + (scl_u64)lane * U;
-#pragma unroll
-        for (int k = 1; k < U; ++k) v[k] = SCL_FUNC(v[k - 1], v[k] SCL_OP_ARGS);
-        const scl_T tot = scl_warp_incl(v[U - 1] SCL_EXTRA_ARGS);
-        scl_T lane_excl = scl_shfl_up(tot, 1);
-        if (lane == 0) lane_excl = ident;
-        const scl_T pre = SCL_FUNC(carry, lane_excl SCL_OP_ARGS);
-#pragma unroll
-        for (int k = 0; k < U; ++k) {
-          const scl_u64 e = e0 + k;
-          if (e < len) {
-            const scl_T r = inclusive ? SCL_FUNC(pre, v[k] SCL_OP_ARGS)
-                                      : (k == 0 ? pre : SCL_FUNC(pre, v[k - 1] SCL_OP_ARGS));
-            out[reverse ? hi - 1 - e : lo + e] = SCL_EPILOGUE(r);
-          }
-        }
-        carry = SCL_FUNC(carry, scl_shfl_idx(tot, 31) SCL_OP_ARGS);
-      }
-    }
-    lo = lo_n;
-    hi = hi_n;
-    lo_n = lo_nn;
-    hi_n = hi_nn;
-#pragma unroll
-    for (int k = 0; k < U; ++k) v[k] = vn[k];
-  }
-}
 #endif

@@ -244,3 +244,184 @@ def test_segmented_pipeline_in_a_graph(scl, orc):
     ref = np.bincount(ids, weights=scan, minlength=len(off) - 1)
     assert np.all(np.abs(replay - ref) <= 1e-5 * np.abs(ref) + 1e-3)
     assert np.allclose(replay, eager, rtol=1e-6)
+
+
+# ---- segment plans: the offsets pre-pass once, one launch per call ----------
+
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+def test_plan_scan_mixed_lengths_exact(scl, orc, flags):
+    """With a plan the segmented Scan is one merged launch (tiles, then a warp
+    per short vector); it gives the pre-pass path's bits and the reference's."""
+    off = mixed_offsets(31)
+    n = int(off[-1])
+    x = orc.mod_i32(n, 32, 1001) - 500
+    p = S.Program(S.KIND_SCAN, IADD, ["int"], identity="0")
+    dx, dy, dz, doff = dev(x), S.DeviceArray(n, np.int32), S.DeviceArray(n, np.int32), dev(off)
+    plan = S.SegPlan(doff, n)
+    p.launch([dx, dy], n=n, flags=flags, segments=plan)
+    p.launch([dx, dz], n=n, flags=flags, segments=doff)
+    want = seg_scan_ref(x, off, flags)
+    assert np.array_equal(dy.to_numpy(), want)
+    assert np.array_equal(dz.to_numpy(), want)
+
+
+def test_plan_reduce_mixed_lengths_exact(scl, orc):
+    off = mixed_offsets(33)
+    n = int(off[-1])
+    x = orc.mod_i32(n, 34, 1001) - 500
+    p = S.Program(S.KIND_REDUCE, IADD, ["int"], identity="0")
+    dout, doff = S.DeviceArray(len(off) - 1, np.int32), dev(off)
+    plan = S.SegPlan(doff, n)
+    ref = np.bincount(seg_ids(off, n), weights=x.astype(np.float64), minlength=len(off) - 1)
+    for _ in range(3):  # the plan's per-vector tickets reset themselves
+        dout.upload(np.zeros(len(off) - 1, np.int32))
+        p.launch([dev(x), dout], n=n, segments=plan)
+        assert np.array_equal(dout.to_numpy().astype(np.int64), ref.astype(np.int64))
+
+
+def test_plan_one_launch_per_call(scl, orc):
+    """After the first call with a tile shape (which numbers the tiles), every
+    segmented Scan and Reduce with the plan is exactly one kernel launch --
+    for short vectors only, long ones only, and a mix."""
+    rng = np.random.default_rng(35)
+    for lens in (rng.integers(1, 200, 100_000), rng.integers(5000, 100_000, 300),
+                 np.concatenate([rng.integers(1, 200, 20_000), rng.integers(5000, 100_000, 50)])):
+        off = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+        n = int(off[-1])
+        x = orc.uniform_f32(n, 36, -1.0, 1.0)
+        sp = S.Program(S.KIND_SCAN, FADD, ["float"], identity="0")
+        rp = S.Program(S.KIND_REDUCE, FADD, ["float"], identity="0")
+        dx, dy, dr, doff = dev(x), S.DeviceArray(n, np.float32), S.DeviceArray(len(lens), np.float32), dev(off)
+        plan = S.SegPlan(doff, n)
+        sp.launch([dx, dy], n=n, flags=S.SHAPE_INCLUSIVE, segments=plan)
+        rp.launch([dx, dr], n=n, segments=plan)
+        for _ in range(3):
+            c0 = S.launch_count()
+            sp.launch([dx, dy], n=n, flags=S.SHAPE_INCLUSIVE, segments=plan)
+            assert S.launch_count() == c0 + 1
+            rp.launch([dx, dr], n=n, segments=plan)
+            assert S.launch_count() == c0 + 2
+        ids = seg_ids(off, n)
+        cs = np.concatenate([[0.0], np.cumsum(x.astype(np.float64))])
+        ref = cs[off[1:].astype(np.int64)] - cs[off[:-1].astype(np.int64)]
+        assert np.all(np.abs(dr.to_numpy() - ref) <= 1e-6 * (1.0 + np.sqrt(lens)))
+        scan = cs[1:] - cs[off[:-1].astype(np.int64)][ids]
+        pos = np.arange(n) - off[:-1].astype(np.int64)[ids] + 1
+        assert np.all(np.abs(dy.to_numpy() - scan) <= 1e-5 * (1.0 + np.sqrt(pos)))
+
+
+def test_plan_on_a_longer_vector_and_misuse(scl, orc):
+    """A plan made for the segments' total serves a longer input (elements
+    past the last vector are left alone); a plan for other segments, or a
+    shorter vector than the plan's, is refused."""
+    off = np.array([0, 3, 3, 10, 5000, 9000], np.uint64)
+    n = 12000
+    x = orc.mod_i32(n, 37, 1001)
+    p = S.Program(S.KIND_REDUCE, IADD, ["int"], identity="0")
+    doff = dev(off)
+    plan = S.SegPlan(doff, int(off[-1]))
+    dout = S.DeviceArray(len(off) - 1, np.int32)
+    p.launch([dev(x), dout], n=n, segments=plan)
+    xs = x.astype(np.int64)
+    assert list(dout.to_numpy()) == [int(xs[int(a):int(b)].sum()) for a, b in zip(off[:-1], off[1:])]
+    other = S.SegPlan(dev(np.array([0, 1, 2], np.uint64)), 2)
+    ptrs = (ctypes.c_void_p * 2)(dev(x).ptr, dout.ptr)
+    sh = S.Shape(n=n, seg_offsets=doff.ptr, n_segments=len(off) - 1, seg_plan=other.id)
+    assert S.lib().scl_launch_reduce(p.handle, ctypes.byref(sh), ptrs, None, 0, None) == S.ERR_ARG
+    sh = S.Shape(n=8000, seg_offsets=doff.ptr, n_segments=len(off) - 1, seg_plan=plan.id)
+    assert S.lib().scl_launch_reduce(p.handle, ctypes.byref(sh), ptrs, None, 0, None) == S.ERR_ARG
+    assert S.lib().scl_segplan_release(123456) == S.ERR_ARG
+
+
+def test_plan_pipeline_in_a_graph(scl, orc):
+    """Map -> segmented Scan -> segmented Reduce with a plan, replayed from a
+    graph twice: one kernel per skeleton in the recording, and the same
+    results on every replay."""
+    off = log_uniform_offsets(3000, 0, 15, seed=38, zeros=30)
+    n = int(off[-1])
+    x = orc.uniform_f32(n, 39, -1.0, 1.0)
+    mp = S.Program(S.KIND_MAP, "float func(float x){ return x*x + 1.0f; }", ["float", "float"])
+    sp = S.Program(S.KIND_SCAN, FADD, ["float"], identity="0")
+    rp = S.Program(S.KIND_REDUCE, FADD, ["float"], identity="0")
+    dx, dm, ds = dev(x), S.DeviceArray(n, np.float32), S.DeviceArray(n, np.float32)
+    dr, doff = S.DeviceArray(len(off) - 1, np.float32), dev(off)
+    plan = S.SegPlan(doff, n)
+
+    def step():
+        mp.launch([dx, dm], n=n)
+        sp.launch([dm, ds], n=n, flags=S.SHAPE_INCLUSIVE, segments=plan)
+        rp.launch([ds, dr], n=n, segments=plan)
+
+    step()
+    eager = dr.to_numpy().copy()
+    c0 = S.launch_count()
+    S.check(S.lib().scl_graph_begin())
+    step()
+    g = ctypes.c_void_p()
+    S.check(S.lib().scl_graph_end(ctypes.byref(g)))
+    assert S.launch_count() == c0 + 3
+    for _ in range(2):
+        dr.upload(np.zeros(len(off) - 1, np.float32))
+        S.check(S.lib().scl_graph_launch(g))
+        S.sync()
+        assert np.allclose(dr.to_numpy(), eager, rtol=1e-6, atol=1e-6)
+    S.check(S.lib().scl_graph_destroy(g))
+
+
+def test_graph_survives_workspace_growth(scl, orc):
+    """A graph records the programs' workspace addresses; a later eager call
+    that needs a larger workspace (or a new scan status layout) must leave
+    the recorded one in place, so the graph replays correctly and the eager
+    calls stay correct too."""
+    n_small = 1_000_003
+    x = orc.mod_i32(4 * n_small, 40, 1001) - 500
+    sp = S.Program(S.KIND_SCAN, IADD, ["int"], identity="0")
+    rp = S.Program(S.KIND_REDUCE, IADD, ["int"], identity="0")
+    dx, dy, dr = dev(x), S.DeviceArray(4 * n_small, np.int32), S.DeviceArray(1, np.int32)
+
+    def small():
+        sp.launch([dx, dy], n=n_small, flags=S.SHAPE_INCLUSIVE)
+        rp.launch([dy, dr], n=n_small)
+
+    small()
+    S.check(S.lib().scl_graph_begin())
+    small()
+    g = ctypes.c_void_p()
+    S.check(S.lib().scl_graph_end(ctypes.byref(g)))
+    # eager calls that grow both workspaces (a longer scan; a segmented reduce)
+    off = mixed_offsets(41)
+    n_big = int(off[-1])
+    assert n_big <= 4 * n_small
+    sp.launch([dx, dy], n=4 * n_small, flags=S.SHAPE_INCLUSIVE)
+    big = dy.to_numpy()
+    assert np.array_equal(big, np.cumsum(x, dtype=np.int32))
+    dseg = S.DeviceArray(len(off) - 1, np.int32)
+    rp.launch([dx, dseg], n=n_big, segments=dev(off))
+    want_small = np.cumsum(x[:n_small], dtype=np.int32)
+    for _ in range(2):
+        dy.upload(np.zeros(4 * n_small, np.int32))
+        S.check(S.lib().scl_graph_launch(g))
+        S.sync()
+        assert np.array_equal(dy.to_numpy()[:n_small], want_small)
+        assert int(dr.to_numpy()[0]) == int(want_small.astype(np.int64).sum() & 0xFFFFFFFF) - \
+            (1 << 32 if (int(want_small.astype(np.int64).sum()) & 0x80000000) else 0)
+    S.check(S.lib().scl_graph_destroy(g))
+    sp.launch([dx, dy], n=4 * n_small, flags=S.SHAPE_INCLUSIVE)
+    assert np.array_equal(dy.to_numpy(), big)
+
+
+def test_flat_reduce_after_planned_segmented_reduce(scl, orc):
+    """One Reduce program used segmented (with a plan) and flat in turn."""
+    off = mixed_offsets(42)
+    n = int(off[-1])
+    x = orc.mod_i32(n, 43, 1001) - 500
+    p = S.Program(S.KIND_REDUCE, IADD, ["int"], identity="0")
+    dx, dseg, dflat = dev(x), S.DeviceArray(len(off) - 1, np.int32), S.DeviceArray(1, np.int32)
+    plan = S.SegPlan(dev(off), n)
+    ref_seg = np.bincount(seg_ids(off, n), weights=x.astype(np.float64), minlength=len(off) - 1)
+    total = int(x.astype(np.int64).sum())
+    for _ in range(3):
+        p.launch([dx, dseg], n=n, segments=plan)
+        p.launch([dx, dflat], n=n)
+        assert np.array_equal(dseg.to_numpy().astype(np.int64), ref_seg.astype(np.int64))
+        assert int(dflat.to_numpy()[0]) == total

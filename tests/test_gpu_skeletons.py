@@ -497,7 +497,9 @@ def test_graph_capture_dot_product(scl, orc):
 
 def test_compile_all_builds_every_variant_up_front(scl, orc):
     """SCL_PROG_COMPILE_ALL: the variants otherwise compiled on first use are
-    built with the program and give the same results."""
+    built with the program (no module is loaded by the launches that pick
+    them) and give the same results."""
+    loads0 = S.debug_counters()["module_loads"]
     n = 100_003
     x = orc.mod_i32(n, 31, 1001)
     rp = S.Program(S.KIND_REDUCE, "int func(int a, int b){ return a + b; }", ["int"], identity="0",
@@ -522,3 +524,10 @@ def test_compile_all_builds_every_variant_up_front(scl, orc):
     for variant, py in ((S.VARIANT_TMA, 8), (S.VARIANT_TMA, 16), (S.VARIANT_LDST, 4), (S.VARIANT_LDST, 8)):
         mo.launch([din, dout], rows=rows, cols=cols, tuning=S.Tuning(variant=variant, tile_h=py))
         assert np.array_equal(dout.to_numpy().reshape(rows, cols), ref), (variant, py)
+    # one module per program, loaded at construction; none on first use
+    assert S.debug_counters()["module_loads"] == loads0 + 3
+    # without the flag the same launches load modules as they go
+    lazy = S.Program(S.KIND_REDUCE, "int func(int a, int b){ return a + b; }", ["int"], identity="0")
+    before = S.debug_counters()["module_loads"]
+    lazy.launch([dx, dr], n=n, tuning=S.Tuning(items=1))
+    assert S.debug_counters()["module_loads"] == before + 1

@@ -35,7 +35,7 @@ def call_noalloc(prog, bufs, n, flags=0, segments=None, n_segments=0):
     ptrs = (ctypes.c_void_p * 2)(*[b.ptr for b in bufs])
     sh = S.Shape(n=n, rows=0, cols=0, dim=0, offset=0,
                  seg_offsets=segments.ptr if segments is not None else None,
-                 n_segments=n_segments, flags=flags, reserved=0)
+                 n_segments=n_segments, flags=flags, seg_plan=0)
     return S.lib().scl_launch_scan_noalloc(prog.handle, ctypes.byref(sh), ptrs, None, 0, None)
 
 
