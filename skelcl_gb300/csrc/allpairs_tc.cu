@@ -111,47 +111,74 @@ __device__ __forceinline__ void raise(unsigned int* err) {
 
 // The split parts live in one [part][row][Kp] bf16 array per operand; rows and
 // Kp are padded to the tile sizes and zero-filled, so every TMA box is in
-// bounds.
-__global__ void split_rows_kernel(const float* __restrict__ X, uint32_t R, uint32_t C, uint32_t Rp,
-                                  uint32_t Cp, int parts, __nv_bfloat16* __restrict__ out) {
-  const uint64_t total = (uint64_t)Rp * Cp;
-  const uint64_t plane = total;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t r = (uint32_t)(i / Cp), c = (uint32_t)(i % Cp);
-    const float x = (r < R && c < C) ? X[(uint64_t)r * C + c] : 0.0f;
-    const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-    const float r1 = x - __bfloat162float(hi);
-    const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
-    out[i] = hi;
-    out[plane + i] = mid;
-    if (parts > 2) out[2 * plane + i] = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+// bounds.  Each thread splits 8 consecutive elements of a row and writes
+// each part's 8 bf16 with one 16-byte store.
+__device__ __forceinline__ void split8(const float (&x)[8], int parts, __nv_bfloat16* o0,
+                                       __nv_bfloat16* o1, __nv_bfloat16* o2) {
+  __align__(16) __nv_bfloat16 h[8], m[8], l[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    h[e] = __float2bfloat16_rn(x[e]);
+    const float r1 = x[e] - __bfloat162float(h[e]);
+    m[e] = __float2bfloat16_rn(r1);
+    l[e] = __float2bfloat16_rn(r1 - __bfloat162float(m[e]));
+  }
+  *reinterpret_cast<uint4*>(o0) = *reinterpret_cast<const uint4*>(h);
+  *reinterpret_cast<uint4*>(o1) = *reinterpret_cast<const uint4*>(m);
+  if (parts > 2) *reinterpret_cast<uint4*>(o2) = *reinterpret_cast<const uint4*>(l);
+}
+
+// X (R x C row-major) -> parts of X ([part][Rp][Cp]): rows over blockIdx.y
+// (grid-stride), 8-element chunks of a row over x.  Cp is a multiple of 64.
+__global__ void __launch_bounds__(256) split_rows_kernel(const float* __restrict__ X, uint32_t R,
+                                                         uint32_t C, uint32_t Rp, uint32_t Cp, int parts,
+                                                         __nv_bfloat16* __restrict__ out) {
+  const uint64_t plane = (uint64_t)Rp * Cp;
+  const uint32_t chunks = Cp / 8;
+  const bool vec = (C % 4u) == 0 && (reinterpret_cast<uintptr_t>(X) & 15u) == 0;
+  for (uint32_t r = blockIdx.y; r < Rp; r += gridDim.y) {
+    for (uint32_t ch = blockIdx.x * blockDim.x + threadIdx.x; ch < chunks; ch += gridDim.x * blockDim.x) {
+      const uint32_t c0 = ch * 8;
+      float x[8];
+      if (r < R && vec && c0 + 8 <= C) {
+        const float4 a = *reinterpret_cast<const float4*>(X + (uint64_t)r * C + c0);
+        const float4 b = *reinterpret_cast<const float4*>(X + (uint64_t)r * C + c0 + 4);
+        x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
+        x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+      } else {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) x[e] = (r < R && c0 + e < C) ? X[(uint64_t)r * C + c0 + e] : 0.0f;
+      }
+      const uint64_t o = (uint64_t)r * Cp + c0;
+      split8(x, parts, out + o, out + plane + o, out + 2 * plane + o);
+    }
   }
 }
 
-// B (K x N row-major) -> parts of B^T ([part][n][Kp]), through 32 x 32 tiles.
-__global__ void split_transpose_kernel(const float* __restrict__ B, uint32_t K, uint32_t N,
-                                       uint32_t Np, uint32_t Kp, int parts,
-                                       __nv_bfloat16* __restrict__ out) {
-  __shared__ float tile[32][33];
-  const uint32_t k0 = blockIdx.y * 32, n0 = blockIdx.x * 32;
+// B (K x N row-major) -> parts of B^T ([part][Np][Kp]) through 64 x 64 tiles
+// in shared memory: coalesced row reads of B, 16-byte stores of 8
+// consecutive k per part.  Np and Kp are multiples of 64.
+__global__ void __launch_bounds__(256) split_transpose_kernel(const float* __restrict__ B, uint32_t K,
+                                                              uint32_t N, uint32_t Np, uint32_t Kp,
+                                                              int parts, __nv_bfloat16* __restrict__ out) {
+  __shared__ float tile[64][65];  // [k][n]
+  const uint32_t k0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
   const uint64_t plane = (uint64_t)Np * Kp;
-  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
-    const uint32_t k = k0 + j, n = n0 + threadIdx.x;
-    tile[j][threadIdx.x] = (k < K && n < N) ? B[(uint64_t)k * N + n] : 0.0f;
+  for (int i = threadIdx.x; i < 64 * 64; i += 256) {
+    const uint32_t kk = (uint32_t)i / 64, nn = (uint32_t)i % 64;
+    const uint32_t k = k0 + kk, n = n0 + nn;
+    tile[kk][nn] = (k < K && n < N) ? B[(uint64_t)k * N + n] : 0.0f;
   }
   __syncthreads();
-  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
-    const uint32_t n = n0 + j, k = k0 + threadIdx.x;
+  for (int i = threadIdx.x; i < 64 * 8; i += 256) {
+    const uint32_t nn = (uint32_t)i / 8, kc = ((uint32_t)i % 8) * 8;
+    const uint32_t n = n0 + nn, k = k0 + kc;
     if (n >= Np || k >= Kp) continue;
-    const float x = tile[threadIdx.x][j];
-    const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-    const float r1 = x - __bfloat162float(hi);
-    const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+    float x[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) x[e] = tile[kc + e][nn];
     const uint64_t o = (uint64_t)n * Kp + k;
-    out[o] = hi;
-    out[plane + o] = mid;
-    if (parts > 2) out[2 * plane + o] = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+    split8(x, parts, out + o, out + plane + o, out + 2 * plane + o);
   }
 }
 
@@ -473,18 +500,18 @@ void split_operands(const float* A, const float* B, uint32_t M, uint32_t N, uint
   uint8_t* s = reinterpret_cast<uint8_t*>(((uintptr_t)scratch + 1023) & ~(uintptr_t)1023);
   __nv_bfloat16* a_parts = reinterpret_cast<__nv_bfloat16*>(s);
   __nv_bfloat16* b_parts = a_parts + (size_t)parts * Mp * Kp;
-  const int sm = rt().sm_count > 0 ? rt().sm_count : 148;
+  auto rows_grid = [](uint32_t Rp, uint32_t Cp) {
+    return dim3((Cp / 8 + 255) / 256, Rp < 65535u ? Rp : 65535u);
+  };
   if (trans & 1) {
-    dim3 agrid((Mp + 31) / 32, (Kp + 31) / 32);
-    tc::split_transpose_kernel<<<agrid, dim3(32, 8), 0, stream>>>(A, K, M, Mp, Kp, parts, a_parts);
+    tc::split_transpose_kernel<<<dim3(Mp / 64, Kp / 64), 256, 0, stream>>>(A, K, M, Mp, Kp, parts, a_parts);
   } else {
-    tc::split_rows_kernel<<<sm * 8, 256, 0, stream>>>(A, M, K, Mp, Kp, parts, a_parts);
+    tc::split_rows_kernel<<<rows_grid(Mp, Kp), 256, 0, stream>>>(A, M, K, Mp, Kp, parts, a_parts);
   }
   if (trans & 2) {
-    tc::split_rows_kernel<<<sm * 8, 256, 0, stream>>>(B, N, K, Np, Kp, parts, b_parts);
+    tc::split_rows_kernel<<<rows_grid(Np, Kp), 256, 0, stream>>>(B, N, K, Np, Kp, parts, b_parts);
   } else {
-    dim3 tgrid((Np + 31) / 32, (Kp + 31) / 32);
-    tc::split_transpose_kernel<<<tgrid, dim3(32, 8), 0, stream>>>(B, K, N, Np, Kp, parts, b_parts);
+    tc::split_transpose_kernel<<<dim3(Np / 64, Kp / 64), 256, 0, stream>>>(B, K, N, Np, Kp, parts, b_parts);
   }
   rt().launches += 2;
   *a_out = a_parts;

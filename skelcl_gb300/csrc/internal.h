@@ -223,12 +223,17 @@ int segments_prepare(const uint64_t* seg_offsets, uint64_t n_seg, uint64_t n_tot
 // Segment plans (segments.cu, scl_segplan_create): the clamped offsets of
 // one segmented vector, the segmented Reduce's per-segment tickets (zero
 // between launches: the last tile of a segment resets its ticket), and per
-// tile shape the tile numbering with its exact tile count.
+// tile shape the tile numbering with its exact tile count and the window
+// records of the short segments.
 struct SegPlanCfg {
   uint64_t tile = 0, vg = 1, a = 0, short_max = 0;
   int reverse = 0;
   unsigned int* tile_start = nullptr;  // device, n_seg + 1
   uint64_t tiles = 0;                  // tile_start[n_seg]
+  // window records of the short segments (device, 4 words each: first
+  // segment, end segment, first element, elements), one block each
+  uint64_t n_rec = 0;
+  uint64_t* win_rec = nullptr;
 };
 struct SegPlan {
   uint32_t id = 0;

@@ -329,7 +329,8 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
   const int V = vec_width(tsz);
   int aligned = aligned16(in) ? 1 : 0;
   if (sh->n_segments && sh->seg_plan) {
-    // a segment plan: one launch, tiles first, then a warp per short segment
+    // a segment plan: one launch, the tiles of the long segments first, then
+    // one block per window of short segments (staged in shared memory)
     SegPlan* pl = segplan_find(sh->seg_plan);
     if (!pl) return fail(SCL_ERR_ARG, "segmented reduce: no segment plan " + std::to_string(sh->seg_plan));
     if (pl->n_seg != sh->n_segments || pl->n_total > n)
@@ -337,26 +338,13 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
     uint64_t n_seg = sh->n_segments;
     const uint32_t R = (tu && tu->items == 8) ? 8 : 32;
     const uint64_t tile = (uint64_t)R * 256 * V;
-    uint64_t short_max = kSegShort;
+    // a window block stages wt elements (32 KB for 16-byte vectors): windows
+    // of wt / 2 and segments of at most wt / 2 elements, so a window's
+    // segments always fit
+    const uint64_t wt = (uint64_t)8 * 256 * V;
+    uint64_t short_max = wt / 2;
     const SegPlanCfg* cfg = nullptr;
     if (int st = segplan_config(pl, tile, 1, 0, 0, short_max, &cfg)) return st;
-    void* offs = pl->off;
-    unsigned int* err = rt().dev_err;
-    if (cfg->tiles == 0) {
-      // every vector short: the warp-per-vector kernel alone (no tile role,
-      // so no register cap from it and more blocks per SM)
-      CUfunction fs = find_kernel(p, "scl_reduce_short<8>");
-      if (!fs) return fail(SCL_ERR_LAUNCH, "kernel scl_reduce_short<8> missing");
-      ArgPack spack;
-      spack.ptrs = {&in, &out, &offs, &n_seg, &short_max};
-      if (int st = pack_extra(p, fs, spack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &spack))
-        return st;
-      uint64_t sb = (n_seg + 7) / 8;
-      const uint64_t smx = (uint64_t)max_resident_blocks(fs, 256, spack.local_bytes);
-      if (sb > smx) sb = smx;
-      p->last_variant = SCL_VARIANT_VECTOR;
-      return launch(fs, dim3((unsigned)std::max<uint64_t>(sb, 1)), dim3(256), 0, spack);
-    }
     const std::string kname = "scl_reduce_seg<" + std::to_string(R) + ", 1>";
     CUfunction fn = find_kernel(p, kname);
     if (!fn) return fail(SCL_ERR_LAUNCH, "kernel " + kname + " missing");
@@ -364,20 +352,21 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
     // there, and it must stay zero between launches
     if (int st = ensure_workspace(p, 256 + cfg->tiles * csz)) return st;
     void* partials = (char*)p->ws.ptr + 256;
+    void* offs = pl->off;
     void* tstart = cfg->tile_start;
     void* tickets = pl->tickets;
+    void* wseg = cfg->win_rec;
+    unsigned int* err = rt().dev_err;
     ArgPack pack;
-    pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max};
+    pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max, &wseg};
     if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
       return st;
-    // warps for the short segments: one per segment, at most what stays resident
-    uint64_t sblocks = (n_seg + 7) / 8;
-    const uint64_t smax = (uint64_t)max_resident_blocks(fn, 256, pack.local_bytes);
-    if (sblocks > smax) sblocks = smax;
-    const uint64_t grid = cfg->tiles + std::max<uint64_t>(sblocks, 1);
+    const uint64_t grid = cfg->tiles + cfg->n_rec;
+    if (grid == 0) return SCL_OK;  // (every vector is either a tile's or in a record)
     if (grid > 0x7fffffffull) return fail(SCL_ERR_ARG, "segmented reduce: too many tiles");
     p->last_variant = SCL_VARIANT_VECTOR;
-    return launch(fn, dim3((unsigned)grid), dim3(256), 0, pack);
+    // (staged elements plus one skipped word in 32)
+    return launch(fn, dim3((unsigned)grid), dim3(256), (wt + wt / 32) * tsz, pack);
   }
   if (sh->n_segments) {
     // one result per segment, one launch (plus the offsets pre-pass)
@@ -425,7 +414,9 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
     if (int st = launch(fn_short, dim3((unsigned)sblocks), dim3(256), 0, spack)) return st;
     // longer segments: tiles (blocks past the last tile return at once)
     ArgPack pack;
-    pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max};
+    void* no_windows = nullptr;
+    pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max,
+                 &no_windows};
     if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
       return st;
     p->last_variant = SCL_VARIANT_VECTOR;
@@ -595,26 +586,11 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   uint64_t tiles;
   const SegPlanCfg* pcfg = nullptr;
   if (plan) {
-    // the plan's exact count
-    if (int st = segplan_config(plan, tile, vg, ga, reverse ? 1 : 0, kSegShort, &pcfg)) return st;
+    // the plan's exact tile count; windows of tile / 2 elements and short
+    // segments of at most tile / 2, so a window's segments fit in one staged
+    // tile
+    if (int st = segplan_config(plan, tile, vg, ga, reverse ? 1 : 0, tile / 2, &pcfg)) return st;
     tiles = pcfg->tiles;
-    if (tiles == 0) {
-      // every vector short: the warp-per-vector kernel alone (no tile role,
-      // so no register cap from it and more blocks per SM)
-      CUfunction fs = find_kernel(p, "scl_scan_short<8>");
-      if (!fs) return fail(SCL_ERR_LAUNCH, "kernel scl_scan_short<8> missing");
-      void* offs = plan->off;
-      uint64_t short_max = kSegShort;
-      ArgPack spack;
-      spack.ptrs = {&in, &out, &offs, &n_seg, &flags, &short_max};
-      if (int st = pack_extra(p, fs, spack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &spack))
-        return st;
-      uint64_t sb = (n_seg + 7) / 8;
-      const uint64_t smx = (uint64_t)max_resident_blocks(fs, 256, spack.local_bytes);
-      if (sb > smx) sb = smx;
-      p->last_variant = SCL_VARIANT_VECTOR;
-      return launch(fs, dim3((unsigned)std::max<uint64_t>(sb, 1)), dim3(256), 0, spack);
-    }
   } else if (n_seg) {
     // an upper bound (the pre-pass has the count): tiles exist only for
     // segments longer than kSegShort, at most n / tile + 2 per such segment
@@ -679,16 +655,16 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   }
   void* seg_off = prepass ? (char*)ws.ptr + total : (plan ? (void*)plan->off : nullptr);
   void* tile_start = prepass ? (char*)ws.ptr + total + seg_of : (plan ? (void*)pcfg->tile_start : nullptr);
-  uint64_t short_max = n_seg ? kSegShort : 0;
+  uint64_t short_max = plan ? pcfg->short_max : (n_seg ? kSegShort : 0);
+  void* win_seg = plan ? (void*)pcfg->win_rec : nullptr;
   uint64_t grid = tiles;
   if (plan) {
-    // the blocks past the tiles scan the short segments, a warp each
-    CUfunction f = find_kernel(p, kname);
-    uint64_t sblocks = (n_seg + 7) / 8;
-    const uint64_t smax = f ? (uint64_t)max_resident_blocks(f, 256, smem) : 1;
-    if (sblocks > smax) sblocks = smax;
-    grid = tiles + std::max<uint64_t>(sblocks, 1);
+    // the blocks past the tiles take one window record of short segments
+    // each; their staged index skips one word in 32
+    grid = tiles + pcfg->n_rec;
+    if (grid == 0) return SCL_OK;  // (every vector is either a tile's or in a record)
     if (grid > 0x7fffffffull) return fail(SCL_ERR_ARG, "segmented scan: too many tiles");
+    smem += smem / 32;
   }
   if (prepass) {
     uint64_t* scratch = reinterpret_cast<uint64_t*>((char*)p->ws.ptr + total + seg_of + seg_ts);
@@ -717,6 +693,7 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
     pack.ptrs.push_back(&tile_start);
     pack.ptrs.push_back(&n_seg);
     pack.ptrs.push_back(&short_max);
+    pack.ptrs.push_back(&win_seg);
   }
   if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
     return st;

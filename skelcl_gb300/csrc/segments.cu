@@ -15,6 +15,7 @@
 // segment once its start (end, for a reverse scan) is rounded onto the grid.
 // Shorter segments, empty ones included, get no tiles: one warp each handles
 // them in a separate kernel.  tile_start[n_segments] is the tile count.
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <map>
@@ -258,7 +259,10 @@ void free_plan(SegPlan* p) {
   cudaFree(p->off);
   cudaFree(p->tickets);
   cudaFree(p->scratch);
-  for (auto& c : p->cfgs) cudaFree(c.tile_start);
+  for (auto& c : p->cfgs) {
+    cudaFree(c.tile_start);
+    cudaFree(c.win_rec);
+  }
 }
 }  // namespace
 
@@ -293,6 +297,47 @@ int segplan_config(SegPlan* p, uint64_t tile, uint64_t vg, uint64_t a, int rever
                                 c.tile_start, p->scratch, rt().stream)) {
     cudaFree(c.tile_start);
     return st;
+  }
+  // Window records of the short segments (on the host, once): consecutive
+  // segments starting in the same window of short_max elements form one
+  // record {first segment, end segment, first element, elements}; a last
+  // segment longer than short_max belongs to the tiles and is left out (its
+  // start ends the record's elements).  All but the last segment of a record
+  // end inside its window, so a record spans at most 2 * short_max elements.
+  // Records whose segments are all empty stay (the Reduce writes their
+  // identities); windows that own no segment get none.
+  std::vector<uint64_t> off(p->n_seg + 1);
+  SCL_CUDA(cudaMemcpyAsync(off.data(), p->off, off.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                           rt().stream));
+  SCL_CUDA(cudaStreamSynchronize(rt().stream));
+  std::vector<uint64_t> rec;
+  for (uint64_t sg = 0; sg < p->n_seg;) {
+    const uint64_t w = off[sg] / short_max, w0 = w * short_max, w1 = w0 + short_max;
+    uint64_t hi = sg + 1;
+    while (hi < p->n_seg && off[hi] >= w0 && off[hi] < w1) ++hi;
+    const uint64_t la = off[hi - 1], lb = std::max(la, off[hi]);
+    const uint64_t top = lb - la > short_max ? hi - 1 : hi;
+    if (top > sg) {
+      const uint64_t e0 = off[sg];
+      uint64_t e1 = top == hi ? lb : off[top];
+      if (e1 < e0) e1 = e0;
+      rec.insert(rec.end(), {sg, top, e0, e1 - e0});
+    }
+    sg = hi;
+  }
+  c.n_rec = rec.size() / 4;
+  if (c.n_rec) {
+    rt().device_allocs++;
+    cudaError_t e = cudaMalloc(&c.win_rec, rec.size() * sizeof(uint64_t));
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c.win_rec, rec.data(), rec.size() * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                          rt().stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(rt().stream);
+    if (e != cudaSuccess) {
+      cudaFree(c.tile_start);
+      cudaFree(c.win_rec);
+      return cuda_fail(e, "segment plan: window records");
+    }
   }
   unsigned int tiles = 0;
   SCL_CUDA(cudaMemcpyAsync(&tiles, c.tile_start + p->n_seg, sizeof(tiles), cudaMemcpyDeviceToHost,

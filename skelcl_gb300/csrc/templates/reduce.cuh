@@ -263,6 +263,116 @@ scl_reduce_short(const scl_T* in, scl_T* out, const scl_u64* seg_off, scl_u64 n_
                           ((scl_u64)gridDim.x * blockDim.x) >> 5 SCL_EXTRA_ARGS);
 }
 
+// Window role of a planned segmented Reduce (the blocks past the tiles):
+// block r takes window record r of the plan, {first vector, end vector,
+// first element, elements}: consecutive vectors of at most short_max elements
+// that start in one window of short_max elements (all but the last end
+// inside it, so the record spans at most 2 * short_max = WT elements).  The
+// elements are staged in shared memory (the index skips one word in 32, so a
+// warp's 32 chunks sit in 32 banks) and folded as one flagged scan (a
+// vector's first element resets the fold, each thread folding WT / 256
+// consecutive positions, then a flagged scan of the threads' folds); each
+// vector's result is the fold at its last element, SCL_IDENTITY for an empty
+// vector.  Folds in the element type, f(earlier, later).
+template <int WT>
+__device__ __forceinline__ void scl_reduce_window_run(const scl_T* in, scl_T* out, const scl_u64* seg_off,
+                                                      const scl_u64* win_rec, scl_u64 r,
+                                                      scl_T* ts SCL_USER_PARAMS) {
+  constexpr int B = 256, C = WT / B, NW = B / 32;
+  static_assert(WT % B == 0 && WT % 32 == 0, "window chunks");
+  __shared__ unsigned int s_head[WT / 32];
+  __shared__ scl_T s_v[2 * NW];
+  __shared__ int s_h[2 * NW];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const scl_T ident = (scl_T)(SCL_IDENTITY);
+  const scl_u64 lo = win_rec[4 * r], top = win_rec[4 * r + 1], e0 = win_rec[4 * r + 2];
+  const scl_u64 ln = win_rec[4 * r + 3];
+  const int len = (int)(ln < (scl_u64)WT ? ln : (scl_u64)WT);  // (more only for bad offsets)
+  auto sx = [](int p) { return p + (p >> 5); };  // staged index
+  for (int k = threadIdx.x; k < WT / 32; k += B) s_head[k] = 0u;
+  __syncthreads();
+  for (scl_u64 sg = lo + threadIdx.x; sg < top; sg += B) {
+    const scl_u64 a = seg_off[sg], b0 = seg_off[sg + 1], b = b0 > a ? b0 : a;
+    if (b == a) {
+      out[sg] = ident;  // an empty vector
+      continue;
+    }
+    if (a < e0 || b > e0 + (scl_u64)len) continue;
+    const unsigned int q = (unsigned int)(a - e0);
+    atomicOr(&s_head[q >> 5], 1u << (q & 31));
+  }
+  if (len == 0) return;  // (block-uniform)
+  for (int p = threadIdx.x; p < len; p += B) ts[sx(p)] = in[e0 + p];
+  __syncthreads();
+  auto head = [&](int q) { return ((s_head[q >> 5] >> (q & 31)) & 1u) != 0; };
+  const int q0 = threadIdx.x * C;
+  scl_T v = ident;
+  bool hd = false;
+  for (int k = 0; k < C; ++k) {
+    const int q = q0 + k;
+    if (q >= len) break;
+    const scl_T x = ts[sx(q)];
+    const bool h = head(q);
+    v = h ? x : SCL_FUNC(v, x SCL_OP_ARGS);
+    hd = hd || h;
+    ts[sx(q)] = v;
+  }
+  // flagged exclusive scan of the threads' (start seen, fold) pairs:
+  // (f1, v1) then (f2, v2) -> (f1 | f2, f2 ? v2 : f(v1, v2))
+  int hf = hd ? 1 : 0;
+  scl_T iv = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const scl_T ov = scl_shfl_up(iv, off);
+    const int oh = __shfl_up_sync(0xffffffffu, hf, off);
+    if (lane >= off) {
+      if (!hf) iv = SCL_FUNC(ov, iv SCL_OP_ARGS);
+      hf |= oh;
+    }
+  }
+  if (lane == 31) {
+    s_v[warp] = iv;
+    s_h[warp] = hf;
+  }
+  scl_T ev = scl_shfl_up(iv, 1);
+  int eh = __shfl_up_sync(0xffffffffu, hf, 1);
+  if (lane == 0) {
+    ev = ident;
+    eh = 0;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    scl_T wv = lane < NW ? s_v[lane] : ident;
+    int wh = lane < NW ? s_h[lane] : 0;
+#pragma unroll
+    for (int off = 1; off < NW; off <<= 1) {
+      const scl_T ov = scl_shfl_up(wv, off);
+      const int oh = __shfl_up_sync(0xffffffffu, wh, off);
+      if (lane >= off) {
+        if (!wh) wv = SCL_FUNC(ov, wv SCL_OP_ARGS);
+        wh |= oh;
+      }
+    }
+    scl_T xv = scl_shfl_up(wv, 1);
+    if (lane == 0) xv = ident;
+    if (lane < NW) s_v[NW + lane] = xv;
+  }
+  __syncthreads();
+  const scl_T carry = eh ? ev : SCL_FUNC(s_v[NW + warp], ev SCL_OP_ARGS);
+  // positions before the chunk's first vector start take the earlier chunks' fold
+  for (int k = 0; k < C; ++k) {
+    const int q = q0 + k;
+    if (q >= len || head(q)) break;
+    ts[sx(q)] = SCL_FUNC(carry, ts[sx(q)] SCL_OP_ARGS);
+  }
+  __syncthreads();
+  for (scl_u64 sg = lo + threadIdx.x; sg < top; sg += B) {
+    const scl_u64 a = seg_off[sg], b0 = seg_off[sg + 1], b = b0 > a ? b0 : a;
+    if (b == a || a < e0 || b > e0 + (scl_u64)len) continue;
+    out[sg] = ts[sx((int)(b - 1 - e0))];
+  }
+}
+
 // Segmented Reduce (no counterpart in the reference): out[s] = the fold of
 // segment [seg_off[s], seg_off[s+1]) of the flat vector, for every segment,
 // in one launch.  Tiles of R x 256 vectors never span segments (segment s
@@ -270,22 +380,25 @@ scl_reduce_short(const scl_T* in, scl_T* out, const scl_u64* seg_off, scl_u64 n_
 // folds its elements into partials[tile], and the last tile of a segment to
 // finish (per-segment ticket, reset afterwards) folds that segment's
 // partials.  An empty segment yields SCL_IDENTITY.  Blocks past the last
-// tile (the grid is an upper bound) return at once; with MERGED they fold
-// the segments of at most short_max elements instead, a warp each
-// (scl_reduce_short_run): one launch for a whole segmented Reduce.
+// tile (the grid is an upper bound) return at once; with MERGED (a segment
+// plan numbered the tiles) they fold the segments of at most short_max
+// elements instead, one window of them per block (scl_reduce_window_run):
+// one launch for a whole segmented Reduce.
 template <int R, int MERGED = 0>
 __global__ void __launch_bounds__(256)
 scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
                const unsigned int* tile_start, scl_u64 n_seg, int aligned, scl_C* partials,
-               unsigned int* tickets, unsigned int* err, scl_u64 short_max SCL_EXTRA_PARAMS) {
+               unsigned int* tickets, unsigned int* err, scl_u64 short_max,
+               const scl_u64* win_rec SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
   (void)short_max;
+  (void)win_rec;
   if constexpr (MERGED != 0) {
     const unsigned int nt = tile_start[n_seg];
-    if (blockIdx.x >= nt) {
-      scl_reduce_short_run<8>(in, out, seg_off, n_seg, short_max,
-                              ((scl_u64)(blockIdx.x - nt) * 256 + threadIdx.x) >> 5,
-                              ((scl_u64)(gridDim.x - nt) * 256) >> 5 SCL_EXTRA_ARGS);
+    if (blockIdx.x >= nt) {  // (block-uniform: the whole block takes the window role)
+      constexpr int WT = 8 * 256 * scl_vec_width<sizeof(scl_T)>::value;  // 32 KB of elements
+      scl_reduce_window_run<WT>(in, out, seg_off, win_rec, blockIdx.x - nt,
+                                reinterpret_cast<scl_T*>(scl_dyn_smem) SCL_EXTRA_ARGS);
       return;
     }
   }

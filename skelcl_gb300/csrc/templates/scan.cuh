@@ -189,8 +189,9 @@ __device__ __forceinline__ int scl_poll(const scl_scan_status& st, long long idx
 // finds an inclusive prefix ends the look-back, otherwise its aggregates are
 // folded in and the next 32 are read.  (Measured on GB300 and not kept:
 // 64 or 128 predecessors per round, several loads in flight per lane, in
-// every round or only after a first round without an inclusive prefix --
-// all slower, 3-18 %.)
+// every round, or only after a first round without an inclusive prefix, or
+// only for the first two waves of tiles -- all slower, 1.5-18 %; with the
+// code present but never taken the time is unchanged.)
 __device__ __forceinline__ scl_C scl_lookback(const scl_scan_status& st, long long tile, long long first,
                                               unsigned int spin_limit, unsigned int* err
                                                   SCL_USER_PARAMS) {
@@ -471,6 +472,140 @@ __device__ __forceinline__ void scl_scan_short_run(const scl_T* in, scl_O* out, 
   }
 }
 
+// Flagged exclusive scan over the block (SCL_SCAN_B threads, in thread
+// order): thread t brings h = "a vector starts in my chunk" and v = the fold
+// of my chunk from its last start (or from its beginning); *carry receives the
+// fold of the earlier chunks back to the nearest start, f(earlier, later).
+// (f1, v1) then (f2, v2) combine to (f1 | f2, f2 ? v2 : f(v1, v2)).
+__device__ __forceinline__ void scl_flag_scan_excl(bool h, scl_T v, scl_T* carry, scl_T* s_v,
+                                                   int* s_h SCL_USER_PARAMS) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const scl_T ident = (scl_T)(SCL_IDENTITY);
+  int hf = h ? 1 : 0;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const scl_T ov = scl_shfl_up(v, off);
+    const int oh = __shfl_up_sync(0xffffffffu, hf, off);
+    if (lane >= off) {
+      if (!hf) v = SCL_FUNC(ov, v SCL_OP_ARGS);
+      hf |= oh;
+    }
+  }
+  if (lane == 31) {
+    s_v[warp] = v;
+    s_h[warp] = hf;
+  }
+  scl_T ev = scl_shfl_up(v, 1);
+  int eh = __shfl_up_sync(0xffffffffu, hf, 1);
+  if (lane == 0) {
+    ev = ident;
+    eh = 0;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    constexpr int NW = SCL_SCAN_B / 32;
+    scl_T wv = lane < NW ? s_v[lane] : ident;
+    int wh = lane < NW ? s_h[lane] : 0;
+#pragma unroll
+    for (int off = 1; off < NW; off <<= 1) {
+      const scl_T ov = scl_shfl_up(wv, off);
+      const int oh = __shfl_up_sync(0xffffffffu, wh, off);
+      if (lane >= off) {
+        if (!wh) wv = SCL_FUNC(ov, wv SCL_OP_ARGS);
+        wh |= oh;
+      }
+    }
+    scl_T xv = scl_shfl_up(wv, 1);
+    int xh = __shfl_up_sync(0xffffffffu, wh, 1);
+    if (lane == 0) {
+      xv = ident;
+      xh = 0;
+    }
+    if (lane < NW) {
+      s_v[NW + lane] = xv;
+      s_h[NW + lane] = xh;
+    }
+  }
+  __syncthreads();
+  const scl_T wv = s_v[SCL_SCAN_B / 32 + warp];
+  *carry = eh ? ev : SCL_FUNC(wv, ev SCL_OP_ARGS);
+}
+
+// Window role of a planned segmented scan (the blocks past the tiles): block
+// r takes window record r of the plan, {first vector, end vector, first
+// element, elements}: consecutive vectors of at most short_max elements that
+// start in one window of short_max elements (all but the last end inside
+// it, so the record spans at most 2 * short_max = TILE elements, one staged
+// tile).  They are staged in shared memory and scanned as one flagged scan
+// (a vector's first element -- its last, for a reverse scan -- resets the
+// fold), each thread folding TILE / 256 consecutive positions (the staged
+// index skips one word in 32, so a warp's 32 chunks sit in 32 banks); the
+// output is written back with coalesced stores.  Carries in the element
+// type, order f(earlier, later), as the tiles.
+template <int TILE>
+__device__ __forceinline__ void scl_scan_window_run(const scl_T* in, scl_O* out, const scl_u64* seg_off,
+                                                    const scl_u64* win_rec, scl_u64 r,
+                                                    unsigned int flags, scl_T* ts SCL_USER_PARAMS) {
+  constexpr int B = SCL_SCAN_B, C = TILE / B;
+  static_assert(TILE % B == 0 && TILE % 32 == 0, "window chunks");
+  __shared__ unsigned int s_head[TILE / 32];
+  __shared__ scl_T s_v[2 * (SCL_SCAN_B / 32)];
+  __shared__ int s_h[2 * (SCL_SCAN_B / 32)];
+  const bool inclusive = (flags & 1u) != 0, reverse = (flags & 2u) != 0;
+  const scl_T ident = (scl_T)(SCL_IDENTITY);
+  const scl_u64 lo = win_rec[4 * r], top = win_rec[4 * r + 1], e0 = win_rec[4 * r + 2];
+  const scl_u64 ln = win_rec[4 * r + 3];
+  const int len = (int)(ln < (scl_u64)TILE ? ln : (scl_u64)TILE);  // (more only for bad offsets)
+  if (len == 0) return;  // (block-uniform) nothing to write for empty vectors
+  auto sx = [](int p) { return p + (p >> 5); };  // staged index
+  for (int k = threadIdx.x; k < TILE / 32; k += B) s_head[k] = 0u;
+  __syncthreads();
+  // heads at logical positions: a vector's first element, or for a reverse
+  // scan its last (logical q <-> physical len - 1 - q)
+  for (scl_u64 sg = lo + threadIdx.x; sg < top; sg += B) {
+    const scl_u64 a = seg_off[sg], b0 = seg_off[sg + 1], b = b0 > a ? b0 : a;
+    if (b == a || a < e0 || b > e0 + (scl_u64)len) continue;
+    const unsigned int q = (unsigned int)(reverse ? e0 + (scl_u64)len - b : a - e0);
+    atomicOr(&s_head[q >> 5], 1u << (q & 31));
+  }
+  for (int p = threadIdx.x; p < len; p += B) ts[sx(p)] = in[e0 + p];
+  __syncthreads();
+  auto head = [&](int q) { return ((s_head[q >> 5] >> (q & 31)) & 1u) != 0; };
+  // each thread folds its chunk of logical positions in place
+  const int q0 = threadIdx.x * C;
+  auto at = [&](int q) { return sx(reverse ? len - 1 - q : q); };
+  scl_T v = ident;
+  bool hd = false;
+  for (int k = 0; k < C; ++k) {
+    const int q = q0 + k;
+    if (q >= len) break;
+    const scl_T x = ts[at(q)];
+    const bool h = head(q);
+    v = h ? x : SCL_FUNC(v, x SCL_OP_ARGS);
+    hd = hd || h;
+    ts[at(q)] = v;
+  }
+  scl_T carry;
+  scl_flag_scan_excl(hd, v, &carry, s_v, s_h SCL_EXTRA_ARGS);
+  // positions before the chunk's first vector start take the earlier chunks' fold
+  for (int k = 0; k < C; ++k) {
+    const int q = q0 + k;
+    if (q >= len || head(q)) break;
+    ts[at(q)] = SCL_FUNC(carry, ts[at(q)] SCL_OP_ARGS);
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < len; p += B) {
+    scl_T res;
+    if (inclusive) {
+      res = ts[sx(p)];
+    } else {
+      const int q = reverse ? len - 1 - p : p;
+      res = head(q) ? ident : ts[sx(reverse ? p + 1 : p - 1)];
+    }
+    out[e0 + p] = SCL_EPILOGUE(res);
+  }
+}
+
 // The warp-per-segment kernel on its own (segmented launches without a
 // segment plan; with one, scl_scan_s<R, MINB, 2> runs the same code in the
 // blocks past the tiles).
@@ -500,18 +635,20 @@ scl_scan_short(const scl_T* in, scl_O* out, const scl_u64* seg_off, scl_u64 n_se
 // tile_start[s] .. tile_start[s+1]-1 (at least one), and the look-back stops
 // at the segment's first tile.  Tickets past the last tile (the grid is an
 // upper bound) return at once.
-// SEG = 2: the same, and the blocks past the tiles scan the segments of at
-// most short_max elements, a warp each (scl_scan_short_run): one launch for
-// a whole segmented scan.
+// SEG = 2: the same (a segment plan numbered the tiles), and the blocks past
+// the tiles scan the segments of at most short_max elements, one window of
+// them per block (scl_scan_window_run): one launch for a whole segmented
+// scan.
 template <int R, int MINB, int SEG = 0>
 __global__ void __launch_bounds__(SCL_SCAN_B, MINB)
 scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int aligned,
            unsigned int* tile_counter, scl_scan_status st, scl_scan_clear clr, unsigned int spin_limit,
            unsigned int* err, const scl_u64* seg_off, const unsigned int* tile_start,
-           scl_u64 n_seg, scl_u64 short_max SCL_EXTRA_PARAMS) {
+           scl_u64 n_seg, scl_u64 short_max, const scl_u64* win_rec SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
   (void)aligned;
   (void)short_max;
+  (void)win_rec;
   constexpr int B = SCL_SCAN_B, W = SCL_SCAN_W;
   constexpr int V = scl_vec_width<sizeof(scl_T)>::value;
   constexpr int TILE = R * B * V;
@@ -541,10 +678,8 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
   scl_scan_clear_other(clr);
   if constexpr (SEG == 2) {
     const unsigned int nt = tile_start[n_seg];
-    if (blockIdx.x >= nt) {  // (block-uniform: no barrier below is reached)
-      scl_scan_short_run<4>(in, out, seg_off, n_seg, flags, short_max,
-                            ((scl_u64)(blockIdx.x - nt) * SCL_SCAN_B + threadIdx.x) >> 5,
-                            ((scl_u64)(gridDim.x - nt) * SCL_SCAN_B) >> 5 SCL_EXTRA_ARGS);
+    if (blockIdx.x >= nt) {  // (block-uniform: the whole block takes the window role)
+      scl_scan_window_run<TILE>(in, out, seg_off, win_rec, blockIdx.x - nt, flags, ts SCL_EXTRA_ARGS);
       return;
     }
   }

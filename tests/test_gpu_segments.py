@@ -374,10 +374,13 @@ def test_graph_survives_workspace_growth(scl, orc):
     the recorded one in place, so the graph replays correctly and the eager
     calls stay correct too."""
     n_small = 1_000_003
-    x = orc.mod_i32(4 * n_small, 40, 1001) - 500
+    off = mixed_offsets(41)
+    n_big = int(off[-1])
+    n_all = max(4 * n_small, n_big)
+    x = orc.mod_i32(n_all, 40, 1001) - 500
     sp = S.Program(S.KIND_SCAN, IADD, ["int"], identity="0")
     rp = S.Program(S.KIND_REDUCE, IADD, ["int"], identity="0")
-    dx, dy, dr = dev(x), S.DeviceArray(4 * n_small, np.int32), S.DeviceArray(1, np.int32)
+    dx, dy, dr = dev(x), S.DeviceArray(n_all, np.int32), S.DeviceArray(1, np.int32)
 
     def small():
         sp.launch([dx, dy], n=n_small, flags=S.SHAPE_INCLUSIVE)
@@ -389,24 +392,21 @@ def test_graph_survives_workspace_growth(scl, orc):
     g = ctypes.c_void_p()
     S.check(S.lib().scl_graph_end(ctypes.byref(g)))
     # eager calls that grow both workspaces (a longer scan; a segmented reduce)
-    off = mixed_offsets(41)
-    n_big = int(off[-1])
-    assert n_big <= 4 * n_small
-    sp.launch([dx, dy], n=4 * n_small, flags=S.SHAPE_INCLUSIVE)
+    sp.launch([dx, dy], n=n_all, flags=S.SHAPE_INCLUSIVE)
     big = dy.to_numpy()
     assert np.array_equal(big, np.cumsum(x, dtype=np.int32))
     dseg = S.DeviceArray(len(off) - 1, np.int32)
     rp.launch([dx, dseg], n=n_big, segments=dev(off))
     want_small = np.cumsum(x[:n_small], dtype=np.int32)
     for _ in range(2):
-        dy.upload(np.zeros(4 * n_small, np.int32))
+        dy.upload(np.zeros(n_all, np.int32))
         S.check(S.lib().scl_graph_launch(g))
         S.sync()
         assert np.array_equal(dy.to_numpy()[:n_small], want_small)
         assert int(dr.to_numpy()[0]) == int(want_small.astype(np.int64).sum() & 0xFFFFFFFF) - \
             (1 << 32 if (int(want_small.astype(np.int64).sum()) & 0x80000000) else 0)
     S.check(S.lib().scl_graph_destroy(g))
-    sp.launch([dx, dy], n=4 * n_small, flags=S.SHAPE_INCLUSIVE)
+    sp.launch([dx, dy], n=n_all, flags=S.SHAPE_INCLUSIVE)
     assert np.array_equal(dy.to_numpy(), big)
 
 
@@ -425,3 +425,39 @@ def test_flat_reduce_after_planned_segmented_reduce(scl, orc):
         p.launch([dx, dflat], n=n)
         assert np.array_equal(dseg.to_numpy().astype(np.int64), ref_seg.astype(np.int64))
         assert int(dflat.to_numpy()[0]) == total
+
+
+def test_plan_double_and_empty_runs(scl, orc):
+    """Planned segmented Scan and Reduce on double (8-byte elements: windows
+    of 2048 elements, longer vectors on tiles), with runs of empty vectors
+    between the others and at both ends: the identity for every empty
+    vector's sum, and each scan against an FP64 reference."""
+    rng = np.random.default_rng(44)
+    lens = np.concatenate([np.zeros(50, np.int64), rng.integers(0, 3000, 3000), np.zeros(200, np.int64),
+                           rng.integers(2040, 2060, 200), rng.integers(3000, 20_000, 40), np.zeros(30, np.int64)])
+    rng.shuffle(lens[50:-30])
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+    n = int(off[-1])
+    x = orc.normal_f32(n, 45).astype(np.float64)
+    sp = S.Program(S.KIND_SCAN, "double func(double a, double b){ return a + b; }", ["double"], identity="0")
+    rp = S.Program(S.KIND_REDUCE, "double func(double a, double b){ return a + b; }", ["double"], identity="0")
+    dx, dy, dr = dev(x), S.DeviceArray(n, np.float64), S.DeviceArray(len(lens), np.float64)
+    plan = S.SegPlan(dev(off), n)
+    ids = seg_ids(off, n)
+    cs = np.concatenate([[0.0], np.cumsum(x)])
+    starts = off[:-1].astype(np.int64)
+    for flags in (S.SHAPE_INCLUSIVE, 0, S.SHAPE_INCLUSIVE | S.SHAPE_REVERSE):
+        sp.launch([dx, dy], n=n, flags=flags, segments=plan)
+        incl = cs[1:] - cs[starts][ids]
+        if flags & S.SHAPE_REVERSE:
+            tot = (cs[off[1:].astype(np.int64)] - cs[starts])[ids]
+            want = tot - incl + x
+        else:
+            want = incl if flags & S.SHAPE_INCLUSIVE else incl - x
+        assert np.allclose(dy.to_numpy(), want, rtol=0, atol=1e-9 * (1 + np.abs(cs).max())), flags
+    dr.upload(np.full(len(lens), 7.0))
+    rp.launch([dx, dr], n=n, segments=plan)
+    got = dr.to_numpy()
+    ref = cs[off[1:].astype(np.int64)] - cs[starts]
+    assert np.all(got[lens == 0] == 0.0)
+    assert np.allclose(got, ref, rtol=0, atol=1e-9 * (1 + np.abs(cs).max()))
