@@ -515,7 +515,7 @@ def secondary(S, oracle, hbm_peak, args):
         "fwd_plus_adjoint_over_fwd": round((fwd + bwd) / fwd, 3),
         "max_abs_err_vs_fp64": float(np.abs(yf - ref).max()),
         "max_abs_prefix": float(np.abs(ref).max()),
-        "note": "about 15 us per call is fixed (status clear, launch, ramp): 2^28 below"}
+        "note": "about 13 us per call is fixed (launch, ramp of the first wave's look-back): 2^28 below"}
     del dxf, dg, dyf, dgx, yf, ref
     n4 = 1 << 28
     hx4 = oracle.uniform_f32(n4, 2, -1.0, 1.0)
@@ -719,8 +719,9 @@ def segmented_short(S, oracle, hbm_peak):
             "reduce": {"ms": round(seg_red, 4), "GBps": round(4 * n / seg_red / 1e6, 1),
                        "flat_ms": round(flat_red, 4), "without_plan_ms": round(np_red, 4),
                        "max_abs_err_vs_fp64_sampled": float(np.abs(sums[pick] - ref).max())},
-            "note": "with a segment plan: one launch per call, vectors of up to 4096 elements a "
-                    "warp each; without it the offsets pre-pass runs on every call"}
+            "note": "with a segment plan: one launch per call, the short vectors in window records "
+                    "staged in shared memory; without it the offsets pre-pass runs on every call and "
+                    "each short vector takes a warp"}
 
 
 def segmented(S, oracle, hbm_peak):
