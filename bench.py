@@ -409,6 +409,12 @@ def secondary(S, oracle, hbm_peak, args):
     zms_h = timed(S, rot(lambda k: zp.launch([pairs[k][0], pairs[k][1], zs[k]], n=n)), 20, 4)
     rms_h = timed(S, rot(lambda k: rp.launch([zs[k], dr], n=n)), 20, 4)
     fms_h = timed(S, rot(lambda k: zr.launch([pairs[k][0], pairs[k][1], dr], n=n)), 20, 4)
+    # the same three with plain launches (no programmatic stream serialization)
+    prev = S.set_overlapped_launches(False)
+    plain = {"zip_ms": timed(S, rot(lambda k: zp.launch([pairs[k][0], pairs[k][1], zs[k]], n=n)), 20, 4),
+             "reduce_ms": timed(S, rot(lambda k: rp.launch([zs[k], dr], n=n)), 20, 4),
+             "fused_ms": timed(S, rot(lambda k: zr.launch([pairs[k][0], pairs[k][1], dr], n=n)), 20, 4)}
+    S.set_overlapped_launches(prev)
     del pairs, zs
     out["dot_product_2^24"] = {
         "zip_GBps": round(12 * n / zms / 1e6, 1), "reduce_GBps": round(4 * n / rms / 1e6, 1),
@@ -424,7 +430,9 @@ def secondary(S, oracle, hbm_peak, args):
                 "fused_ms": round(fms_h, 4), "fused_GBps": round(8 * n / fms_h / 1e6, 1),
                 "fused_frac": round(8 * n / fms_h / 1e6 / hbm_peak, 3),
                 "unfused_ms": round(zms_h + rms_h, 4),
-                "note": "inputs rotating through four pairs (1 GiB): no L2 reuse between iterations"},
+                "plain_launches": {k: round(v, 4) for k, v in plain.items()},
+                "note": "inputs rotating through four pairs (1 GiB): no L2 reuse between iterations; "
+                        "'plain_launches': the same without programmatic stream serialization"},
         "note": "top-level figures: the same 128 MiB of inputs every iteration (about L2 size, "
                 "so they include L2 reuse); 'hbm': rotating inputs"}
     del da, db, dz, dr

@@ -368,6 +368,18 @@ int scl_autotune_get(int* mode);
 int scl_program_last_variant(const scl_program* prog, uint32_t* variant);
 /* Kernels this library launched since scl_init (all programs). */
 int scl_launch_count(uint64_t* count);
+/* Overlapped launches (no counterpart in the reference).  Skeleton kernels
+ * are launched with programmatic stream serialization: a kernel's blocks may
+ * be scheduled while the previous kernel on the library stream drains, and
+ * each block first waits (griddepcontrol.wait) until that kernel has
+ * completed, so results are the same; what is saved is the launch gap
+ * between dependent kernels (about 2 us a launch).  On by default;
+ * SKELCL_PDL=0 at scl_init, or scl_pdl_set(0), launches them plainly.
+ * *previous (may be NULL) receives the earlier setting. */
+int scl_pdl_set(int enable, int* previous);
+/* Skeleton launches made with programmatic stream serialization since
+ * scl_init. */
+int scl_pdl_launch_count(uint64_t* count);
 /* Device allocations the library has made since scl_init (scl_alloc and its
  * own scratch) and cubins it has loaded; for tests that check a call
  * allocates or loads nothing.  No counterpart in the reference. */

@@ -103,6 +103,8 @@ SIGNATURES = {
     "scl_launch_mapoverlap": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_allpairs": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_count": ([ctypes.POINTER(_U64)], _I),
+    "scl_pdl_set": ([ctypes.c_int, ctypes.POINTER(ctypes.c_int)], _I),
+    "scl_pdl_launch_count": ([ctypes.POINTER(_U64)], _I),
     "scl_debug_counters": ([ctypes.POINTER(_U64), ctypes.POINTER(_U64)], _I),
     "scl_debug_fp32_peak": ([_I, _U32, _VP, _U64, ctypes.POINTER(_U64)], _I),
     "scl_debug_allpairs_split": ([_VP, _VP, _U32, _U32, _U32, _I, _I, _VP, _SZ, ctypes.POINTER(_SZ)], _I),
@@ -156,6 +158,21 @@ def sync() -> None:
 def launch_count() -> int:
     v = ctypes.c_uint64(0)
     check(lib().scl_launch_count(ctypes.byref(v)))
+    return v.value
+
+
+def set_overlapped_launches(enable: bool) -> bool:
+    """Launch skeleton kernels with programmatic stream serialization (the
+    default) or plainly; returns the previous setting."""
+    prev = ctypes.c_int(0)
+    check(lib().scl_pdl_set(1 if enable else 0, ctypes.byref(prev)))
+    return bool(prev.value)
+
+
+def overlapped_launch_count() -> int:
+    """Skeleton launches made with programmatic stream serialization."""
+    v = ctypes.c_uint64(0)
+    check(lib().scl_pdl_launch_count(ctypes.byref(v)))
     return v.value
 
 

@@ -46,6 +46,7 @@ struct Driver {
   CUresult (*cuLaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned,
                              unsigned, unsigned, unsigned, CUstream, void**,
                              void**) = nullptr;
+  CUresult (*cuLaunchKernelEx)(const CUlaunchConfig*, CUfunction, void**, void**) = nullptr;
   CUresult (*cuOccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int,
                                                           size_t) = nullptr;
   CUresult (*cuFuncGetParamInfo)(CUfunction, size_t, size_t*, size_t*) = nullptr;
@@ -72,6 +73,12 @@ struct Runtime {
   unsigned int* dev_err = nullptr;   // device-side status word
   unsigned int* host_err = nullptr;  // pinned mirror
   uint64_t launches = 0;
+  // Template kernels are launched with programmatic stream serialization: a
+  // kernel's blocks may be scheduled while the previous kernel in the stream
+  // drains, and each waits (griddepcontrol.wait, its first statement) until
+  // that kernel has completed.  Off with SKELCL_PDL=0 or scl_pdl_set(0).
+  bool pdl = true;
+  uint64_t pdl_launches = 0;
   uint64_t device_allocs = 0;  // device allocations made by the library (scl_alloc included)
   uint64_t module_loads = 0;   // cubins loaded
   bool capturing = false;

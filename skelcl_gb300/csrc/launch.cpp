@@ -141,9 +141,35 @@ int launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, ArgPack& pack) {
                                              (int)smem);
     if (r != CUDA_SUCCESS) return cu_fail(r, "cuFuncSetAttribute(max dynamic smem)");
   }
+  void** params = pack.ptrs.empty() ? nullptr : pack.ptrs.data();
+  if (rt().pdl) {
+    // Programmatic stream serialization: this grid may be scheduled while the
+    // previous kernel of the stream drains; every template kernel's first
+    // statement (SCL_EXTRA_SETUP) waits for that kernel's completion.
+    CUlaunchAttribute attr;
+    std::memset(&attr, 0, sizeof(attr));
+    attr.id = CU_LAUNCH_ATTRIBUTE_PROGRAMMATIC_STREAM_SERIALIZATION;
+    attr.value.programmaticStreamSerializationAllowed = 1;
+    CUlaunchConfig cfg;
+    std::memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDimX = grid.x;
+    cfg.gridDimY = grid.y;
+    cfg.gridDimZ = grid.z;
+    cfg.blockDimX = block.x;
+    cfg.blockDimY = block.y;
+    cfg.blockDimZ = block.z;
+    cfg.sharedMemBytes = (unsigned)smem;
+    cfg.hStream = (CUstream)rt().stream;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    CUresult r = rt().drv.cuLaunchKernelEx(&cfg, fn, params, nullptr);
+    if (r != CUDA_SUCCESS) return cu_fail(r, "cuLaunchKernelEx");
+    ++rt().launches;
+    ++rt().pdl_launches;
+    return SCL_OK;
+  }
   CUresult r = rt().drv.cuLaunchKernel(fn, grid.x, grid.y, grid.z, block.x, block.y, block.z,
-                                       (unsigned)smem, (CUstream)rt().stream,
-                                       pack.ptrs.empty() ? nullptr : pack.ptrs.data(), nullptr);
+                                       (unsigned)smem, (CUstream)rt().stream, params, nullptr);
   if (r != CUDA_SUCCESS) return cu_fail(r, "cuLaunchKernel");
   ++rt().launches;
   return SCL_OK;

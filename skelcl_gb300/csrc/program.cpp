@@ -315,7 +315,7 @@ int assemble(const scl_program_desc* d, scl_program* p, bool want_f64, Assembly*
   }
   s << "#define SCL_EXTRA_PARAMS " << em.params << "\n"
     << "#define SCL_USER_PARAMS " << em.user << "\n"
-    << "#define SCL_EXTRA_SETUP " << em.setup << "\n"
+    << "#define SCL_EXTRA_SETUP SCL_GRID_DEPENDENCY_WAIT " << em.setup << "\n"
     << "#define SCL_EXTRA_ARGS " << em.args << "\n"
     << "#define SCL_REDUCE_ARGS " << reduce_args << "\n"
     << "#define SCL_ZIP_ARGS " << zip_args << "\n";

@@ -150,6 +150,7 @@ extern "C" int scl_init(int device) {
   if (int st = resolve("cuFuncSetAttribute", &d.cuFuncSetAttribute)) return st;
   if (int st = resolve("cuFuncGetAttribute", &d.cuFuncGetAttribute)) return st;
   if (int st = resolve("cuLaunchKernel", &d.cuLaunchKernel)) return st;
+  if (resolve("cuLaunchKernelEx", &d.cuLaunchKernelEx) != SCL_OK) d.cuLaunchKernelEx = nullptr;
   if (int st = resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor",
                        &d.cuOccupancyMaxActiveBlocksPerMultiprocessor))
     return st;
@@ -178,6 +179,11 @@ extern "C" int scl_init(int device) {
   SCL_CUDA(cudaMallocHost(&g_rt.host_err, 64));
   std::memset(g_rt.host_err, 0, 64);
   g_rt.launches = 0;
+  g_rt.pdl_launches = 0;
+  {
+    const char* e = std::getenv("SKELCL_PDL");
+    g_rt.pdl = d.cuLaunchKernelEx != nullptr && !(e && std::string(e) == "0");
+  }
   g_rt.initialized = true;
   return SCL_OK;
 }
@@ -430,6 +436,21 @@ extern "C" int scl_graph_destroy(scl_graph* g) {
 extern "C" int scl_launch_count(uint64_t* count) {
   if (!count) return fail(SCL_ERR_ARG, "null argument");
   *count = g_rt.launches;
+  return SCL_OK;
+}
+
+extern "C" int scl_pdl_set(int enable, int* previous) {
+  if (int st = require_init()) return st;
+  if (previous) *previous = g_rt.pdl ? 1 : 0;
+  if (enable && !g_rt.drv.cuLaunchKernelEx)
+    return fail(SCL_ERR_ARG, "this driver has no cuLaunchKernelEx: launches cannot overlap");
+  g_rt.pdl = enable != 0;
+  return SCL_OK;
+}
+
+extern "C" int scl_pdl_launch_count(uint64_t* count) {
+  if (!count) return fail(SCL_ERR_ARG, "null argument");
+  *count = g_rt.pdl_launches;
   return SCL_OK;
 }
 

@@ -44,6 +44,14 @@ typedef long long scl_i64;
 
 extern __shared__ __align__(128) unsigned char scl_dyn_smem[];
 
+// Every template kernel's first statement is SCL_EXTRA_SETUP, which begins
+// with this wait.  The host launches template kernels with programmatic
+// stream serialization, so a grid may be scheduled before the previous
+// kernel of the stream has finished; griddepcontrol.wait returns once that
+// kernel has completed and its writes are visible (at once for a launch
+// without the attribute).  Nothing before it touches global memory.
+#define SCL_GRID_DEPENDENCY_WAIT asm volatile("griddepcontrol.wait;" ::: "memory");
+
 __device__ __forceinline__ unsigned scl_cl_dim(unsigned d) {
   return SCL_WI_SWAP ? (d == 0u ? 1u : (d == 1u ? 0u : d)) : d;
 }

@@ -206,3 +206,26 @@ def test_compile_errors_are_reported(built):
 def test_custom_func_name_and_comments(built):
     src = "/* helper */ float sq(float v) { return v*v; }\n// the entry\nfloat myfn(float f) { return sq(f) + 1.0f; }"
     s.compile_only(s.KIND_MAP, src, ["float", "float"], func="myfn")
+
+
+def test_every_template_kernel_waits_for_its_predecessor():
+    """Skeleton kernels are launched with programmatic stream serialization,
+    which is only safe when each kernel's first statement waits for the
+    previous grid: every __global__ in the templates must open with
+    SCL_EXTRA_SETUP, and the generated SCL_EXTRA_SETUP must begin with the
+    griddepcontrol.wait of the prelude."""
+    tdir = ROOT / "skelcl_gb300" / "csrc" / "templates"
+    kernels = 0
+    for f in sorted(tdir.glob("*.cuh")):
+        text = f.read_text()
+        for m in re.finditer(r"__global__", text):
+            body = text.index("{", m.end())
+            first = text[body + 1:body + 400].strip().splitlines()[0].strip()
+            line = text[:m.start()].count("\n") + 1
+            assert first.startswith("SCL_EXTRA_SETUP"), f"{f.name}:{line} opens with {first!r}"
+            kernels += 1
+    assert kernels >= 25
+    prelude = (tdir / "prelude.cuh").read_text()
+    assert re.search(r'#define SCL_GRID_DEPENDENCY_WAIT asm volatile\("griddepcontrol\.wait;"', prelude)
+    prog = (ROOT / "skelcl_gb300" / "csrc" / "program.cpp").read_text()
+    assert '"#define SCL_EXTRA_SETUP SCL_GRID_DEPENDENCY_WAIT "' in prog
