@@ -327,6 +327,52 @@ struct scl_vec_width {
                                 16 % S1 == 0 && 16 % S2 == 0) ? 16 / S : 1;
 };
 
+// Segment-plan windows: a vector of at most this many elements is folded or
+// scanned by one thread, a longer one by a warp.
+#define SCL_WIN_THREAD 256
+
+// Copies the 16-byte-aligned vectors covering src[0 .. len) (len <= MAXLEN)
+// to ts as they are, so that src[p] lands at ts[p + shift]; returns shift
+// (the elements of the first vector that lie before src).  CH vectors per
+// thread are in flight before any is stored; ts needs MAXLEN + 16 / sizeof(T)
+// elements and 16-byte alignment.  The first and last vectors may hold
+// elements outside the range (an aligned 16-byte vector lies within one page
+// of the buffer that holds its in-range elements).  Elements that do not
+// tile 16 bytes, or do not sit on their own size, are copied one by one
+// (shift 0).
+template <typename T, int MAXLEN, int B, int CH>
+__device__ __forceinline__ int scl_stage_aligned(const T* src, int len, T* ts) {
+  constexpr int V = scl_vec_width<sizeof(T)>::value;
+  const unsigned long long addr = (unsigned long long)src;
+  if constexpr (V == 1) {
+    for (int p = threadIdx.x; p < len; p += B) ts[p] = src[p];
+    return 0;
+  }
+  if (addr % sizeof(T) != 0) {
+    for (int p = threadIdx.x; p < len; p += B) ts[p] = src[p];
+    return 0;
+  }
+  const int mis = (int)((addr & 15u) / sizeof(T));
+  const T* base = src - mis;
+  const int nv = len > 0 ? (mis + len + V - 1) / V : 0;
+  constexpr int PER = (MAXLEN + V - 1) / V / B + 1;  // vectors per thread at most
+#pragma unroll
+  for (int k0 = 0; k0 < PER; k0 += CH) {
+    scl_pack<T, V> buf[CH];
+#pragma unroll
+    for (int k = 0; k < CH; ++k) {
+      const int v = threadIdx.x + (k0 + k) * B;
+      if (k0 + k < PER && v < nv) buf[k] = scl_load<T, V>(base + (scl_u64)v * V);
+    }
+#pragma unroll
+    for (int k = 0; k < CH; ++k) {
+      const int v = threadIdx.x + (k0 + k) * B;
+      if (k0 + k < PER && v < nv) scl_store<T, V>(ts + v * V, buf[k]);
+    }
+  }
+  return mis;
+}
+
 // Device-side status word: bit 0 = a bounded wait gave up.
 #define SCL_DEV_ERR_TIMEOUT 1u
 __device__ __forceinline__ void scl_raise(unsigned int* err, unsigned int bit) {

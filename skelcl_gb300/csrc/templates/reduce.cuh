@@ -268,108 +268,84 @@ scl_reduce_short(const scl_T* in, scl_T* out, const scl_u64* seg_off, scl_u64 n_
 // first element, elements}: consecutive vectors of at most short_max elements
 // that start in one window of short_max elements (all but the last end
 // inside it, so the record spans at most 2 * short_max = WT elements).  The
-// elements are staged in shared memory (the index skips one word in 32, so a
-// warp's 32 chunks sit in 32 banks) and folded as one flagged scan (a
-// vector's first element resets the fold, each thread folding WT / 256
-// consecutive positions, then a flagged scan of the threads' folds); each
-// vector's result is the fold at its last element, SCL_IDENTITY for an empty
-// vector.  Folds in the element type, f(earlier, later).
+// 16-byte vectors covering the record's elements are copied to shared memory
+// as they are (element e0 + p at ts[p + shift]).  Then a vector of at most
+// SCL_WIN_THREAD elements is folded by one thread (four interleaved folds of
+// the elements e = 0, 1, 2, 3 mod 4, combined at the end; in element order
+// below 8 elements); a longer one by a warp: lane l folds elements l, l + 32, ... in order and the
+// lanes' folds combine in a shuffle tree (a strided fold and a tree, as in
+// the flat reduce; the operator is taken to be commutative), each warp
+// reading the offsets of its next 32 vectors at once.  An empty vector
+// yields SCL_IDENTITY.  Folds in the element type.
 template <int WT>
 __device__ __forceinline__ void scl_reduce_window_run(const scl_T* in, scl_T* out, const scl_u64* seg_off,
                                                       const scl_u64* win_rec, scl_u64 r,
                                                       scl_T* ts SCL_USER_PARAMS) {
-  constexpr int B = 256, C = WT / B, NW = B / 32;
-  static_assert(WT % B == 0 && WT % 32 == 0, "window chunks");
-  __shared__ unsigned int s_head[WT / 32];
-  __shared__ scl_T s_v[2 * NW];
-  __shared__ int s_h[2 * NW];
+  constexpr int B = 256, NW = B / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const scl_T ident = (scl_T)(SCL_IDENTITY);
   const scl_u64 lo = win_rec[4 * r], top = win_rec[4 * r + 1], e0 = win_rec[4 * r + 2];
   const scl_u64 ln = win_rec[4 * r + 3];
   const int len = (int)(ln < (scl_u64)WT ? ln : (scl_u64)WT);  // (more only for bad offsets)
-  auto sx = [](int p) { return p + (p >> 5); };  // staged index
-  for (int k = threadIdx.x; k < WT / 32; k += B) s_head[k] = 0u;
+  const int shift = scl_stage_aligned<scl_T, WT, B, 4>(in + e0, len, ts);
   __syncthreads();
+  // short vectors (and empty ones): a thread each
   for (scl_u64 sg = lo + threadIdx.x; sg < top; sg += B) {
     const scl_u64 a = seg_off[sg], b0 = seg_off[sg + 1], b = b0 > a ? b0 : a;
     if (b == a) {
-      out[sg] = ident;  // an empty vector
+      out[sg] = ident;
       continue;
     }
-    if (a < e0 || b > e0 + (scl_u64)len) continue;
-    const unsigned int q = (unsigned int)(a - e0);
-    atomicOr(&s_head[q >> 5], 1u << (q & 31));
-  }
-  if (len == 0) return;  // (block-uniform)
-  for (int p = threadIdx.x; p < len; p += B) ts[sx(p)] = in[e0 + p];
-  __syncthreads();
-  auto head = [&](int q) { return ((s_head[q >> 5] >> (q & 31)) & 1u) != 0; };
-  const int q0 = threadIdx.x * C;
-  scl_T v = ident;
-  bool hd = false;
-  for (int k = 0; k < C; ++k) {
-    const int q = q0 + k;
-    if (q >= len) break;
-    const scl_T x = ts[sx(q)];
-    const bool h = head(q);
-    v = h ? x : SCL_FUNC(v, x SCL_OP_ARGS);
-    hd = hd || h;
-    ts[sx(q)] = v;
-  }
-  // flagged exclusive scan of the threads' (start seen, fold) pairs:
-  // (f1, v1) then (f2, v2) -> (f1 | f2, f2 ? v2 : f(v1, v2))
-  int hf = hd ? 1 : 0;
-  scl_T iv = v;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const scl_T ov = scl_shfl_up(iv, off);
-    const int oh = __shfl_up_sync(0xffffffffu, hf, off);
-    if (lane >= off) {
-      if (!hf) iv = SCL_FUNC(ov, iv SCL_OP_ARGS);
-      hf |= oh;
-    }
-  }
-  if (lane == 31) {
-    s_v[warp] = iv;
-    s_h[warp] = hf;
-  }
-  scl_T ev = scl_shfl_up(iv, 1);
-  int eh = __shfl_up_sync(0xffffffffu, hf, 1);
-  if (lane == 0) {
-    ev = ident;
-    eh = 0;
-  }
-  __syncthreads();
-  if (warp == 0) {
-    scl_T wv = lane < NW ? s_v[lane] : ident;
-    int wh = lane < NW ? s_h[lane] : 0;
-#pragma unroll
-    for (int off = 1; off < NW; off <<= 1) {
-      const scl_T ov = scl_shfl_up(wv, off);
-      const int oh = __shfl_up_sync(0xffffffffu, wh, off);
-      if (lane >= off) {
-        if (!wh) wv = SCL_FUNC(ov, wv SCL_OP_ARGS);
-        wh |= oh;
+    if (b - a > SCL_WIN_THREAD || a < e0 || b > e0 + (scl_u64)len) continue;
+    const scl_T* v = ts + (int)(a - e0) + shift;
+    const int nv = (int)(b - a);
+    scl_T acc;
+    if (nv < 8) {
+      acc = v[0];
+      for (int e = 1; e < nv; ++e) acc = SCL_FUNC(acc, v[e] SCL_OP_ARGS);
+    } else {
+      // four interleaved folds (elements e = j mod 4), then combined
+      scl_T c0 = v[0], c1 = v[1], c2 = v[2], c3 = v[3];
+      int e = 4;
+      for (; e + 3 < nv; e += 4) {
+        c0 = SCL_FUNC(c0, v[e] SCL_OP_ARGS);
+        c1 = SCL_FUNC(c1, v[e + 1] SCL_OP_ARGS);
+        c2 = SCL_FUNC(c2, v[e + 2] SCL_OP_ARGS);
+        c3 = SCL_FUNC(c3, v[e + 3] SCL_OP_ARGS);
       }
+      if (e < nv) c0 = SCL_FUNC(c0, v[e] SCL_OP_ARGS);
+      if (e + 1 < nv) c1 = SCL_FUNC(c1, v[e + 1] SCL_OP_ARGS);
+      if (e + 2 < nv) c2 = SCL_FUNC(c2, v[e + 2] SCL_OP_ARGS);
+      acc = SCL_FUNC(SCL_FUNC(c0, c1 SCL_OP_ARGS), SCL_FUNC(c2, c3 SCL_OP_ARGS) SCL_OP_ARGS);
     }
-    scl_T xv = scl_shfl_up(wv, 1);
-    if (lane == 0) xv = ident;
-    if (lane < NW) s_v[NW + lane] = xv;
+    out[sg] = acc;
   }
-  __syncthreads();
-  const scl_T carry = eh ? ev : SCL_FUNC(s_v[NW + warp], ev SCL_OP_ARGS);
-  // positions before the chunk's first vector start take the earlier chunks' fold
-  for (int k = 0; k < C; ++k) {
-    const int q = q0 + k;
-    if (q >= len || head(q)) break;
-    ts[sx(q)] = SCL_FUNC(carry, ts[sx(q)] SCL_OP_ARGS);
-  }
-  __syncthreads();
-  for (scl_u64 sg = lo + threadIdx.x; sg < top; sg += B) {
-    const scl_u64 a = seg_off[sg], b0 = seg_off[sg + 1], b = b0 > a ? b0 : a;
-    if (b == a || a < e0 || b > e0 + (scl_u64)len) continue;
-    out[sg] = ts[sx((int)(b - 1 - e0))];
+  // longer vectors: warp w takes vectors lo + w, lo + w + NW, ... (its next
+  // 32 offset pairs read at once, one per lane)
+  for (scl_u64 g = lo + warp; g < top; g += (scl_u64)NW * 32) {
+    const scl_u64 mine = g + (scl_u64)NW * lane;
+    scl_u64 a_l = 0, b_l = 0;
+    if (mine < top) {
+      a_l = seg_off[mine];
+      b_l = seg_off[mine + 1];
+    }
+    const int cnt = (int)((top - g + NW - 1) / NW < 32 ? (top - g + NW - 1) / NW : 32);
+    for (int k = 0; k < cnt; ++k) {
+      const scl_u64 sg = g + (scl_u64)NW * k;
+      const scl_u64 a = __shfl_sync(0xffffffffu, a_l, k), b0 = __shfl_sync(0xffffffffu, b_l, k);
+      const scl_u64 b = b0 > a ? b0 : a;
+      if (b - a <= SCL_WIN_THREAD) continue;  // (a thread's, above)
+      if (a < e0 || b > e0 + (scl_u64)len) continue;  // (only for offsets changed since the plan)
+      const int pa = (int)(a - e0) + shift, pb = (int)(b - e0) + shift;
+      scl_T acc = ts[pa + lane];  // (every lane has an element: more than 32 of them)
+      for (int p = pa + lane + 32; p < pb; p += 32) acc = SCL_FUNC(acc, ts[p] SCL_OP_ARGS);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const scl_T o = scl_shfl_down(acc, off);
+        if (lane + off < 32) acc = SCL_FUNC(acc, o SCL_OP_ARGS);
+      }
+      if (lane == 0) out[sg] = acc;
+    }
   }
 }
 

@@ -472,138 +472,98 @@ __device__ __forceinline__ void scl_scan_short_run(const scl_T* in, scl_O* out, 
   }
 }
 
-// Flagged exclusive scan over the block (SCL_SCAN_B threads, in thread
-// order): thread t brings h = "a vector starts in my chunk" and v = the fold
-// of my chunk from its last start (or from its beginning); *carry receives the
-// fold of the earlier chunks back to the nearest start, f(earlier, later).
-// (f1, v1) then (f2, v2) combine to (f1 | f2, f2 ? v2 : f(v1, v2)).
-__device__ __forceinline__ void scl_flag_scan_excl(bool h, scl_T v, scl_T* carry, scl_T* s_v,
-                                                   int* s_h SCL_USER_PARAMS) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const scl_T ident = (scl_T)(SCL_IDENTITY);
-  int hf = h ? 1 : 0;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const scl_T ov = scl_shfl_up(v, off);
-    const int oh = __shfl_up_sync(0xffffffffu, hf, off);
-    if (lane >= off) {
-      if (!hf) v = SCL_FUNC(ov, v SCL_OP_ARGS);
-      hf |= oh;
-    }
-  }
-  if (lane == 31) {
-    s_v[warp] = v;
-    s_h[warp] = hf;
-  }
-  scl_T ev = scl_shfl_up(v, 1);
-  int eh = __shfl_up_sync(0xffffffffu, hf, 1);
-  if (lane == 0) {
-    ev = ident;
-    eh = 0;
-  }
-  __syncthreads();
-  if (warp == 0) {
-    constexpr int NW = SCL_SCAN_B / 32;
-    scl_T wv = lane < NW ? s_v[lane] : ident;
-    int wh = lane < NW ? s_h[lane] : 0;
-#pragma unroll
-    for (int off = 1; off < NW; off <<= 1) {
-      const scl_T ov = scl_shfl_up(wv, off);
-      const int oh = __shfl_up_sync(0xffffffffu, wh, off);
-      if (lane >= off) {
-        if (!wh) wv = SCL_FUNC(ov, wv SCL_OP_ARGS);
-        wh |= oh;
-      }
-    }
-    scl_T xv = scl_shfl_up(wv, 1);
-    int xh = __shfl_up_sync(0xffffffffu, wh, 1);
-    if (lane == 0) {
-      xv = ident;
-      xh = 0;
-    }
-    if (lane < NW) {
-      s_v[NW + lane] = xv;
-      s_h[NW + lane] = xh;
-    }
-  }
-  __syncthreads();
-  const scl_T wv = s_v[SCL_SCAN_B / 32 + warp];
-  *carry = eh ? ev : SCL_FUNC(wv, ev SCL_OP_ARGS);
-}
-
 // Window role of a planned segmented scan (the blocks past the tiles): block
 // r takes window record r of the plan, {first vector, end vector, first
 // element, elements}: consecutive vectors of at most short_max elements that
 // start in one window of short_max elements (all but the last end inside
 // it, so the record spans at most 2 * short_max = TILE elements, one staged
-// tile).  They are staged in shared memory and scanned as one flagged scan
-// (a vector's first element -- its last, for a reverse scan -- resets the
-// fold), each thread folding TILE / 256 consecutive positions (the staged
-// index skips one word in 32, so a warp's 32 chunks sit in 32 banks); the
-// output is written back with coalesced stores.  Carries in the element
-// type, order f(earlier, later), as the tiles.
+// tile).  The 16-byte vectors covering the record's elements are copied to
+// shared memory as they are (element e0 + p at ts[p + shift]) and every
+// vector is scanned in place there: one of at most SCL_WIN_THREAD elements by
+// one thread, in element order; a longer one by a warp, in rounds of 32 x U
+// logical elements (lane l holds U consecutive ones; a reverse scan reads the
+// vector from its end), the lanes' totals scanned across the warp and rounds
+// chained by a carry.  Then the block stores the record's elements in order
+// (the vectors cover them).  f(earlier, later) throughout, in the element
+// type; the exclusive form starts from SCL_IDENTITY (neutral, as for the
+// tiles' padding).
 template <int TILE>
 __device__ __forceinline__ void scl_scan_window_run(const scl_T* in, scl_O* out, const scl_u64* seg_off,
                                                     const scl_u64* win_rec, scl_u64 r,
                                                     unsigned int flags, scl_T* ts SCL_USER_PARAMS) {
-  constexpr int B = SCL_SCAN_B, C = TILE / B;
-  static_assert(TILE % B == 0 && TILE % 32 == 0, "window chunks");
-  __shared__ unsigned int s_head[TILE / 32];
-  __shared__ scl_T s_v[2 * (SCL_SCAN_B / 32)];
-  __shared__ int s_h[2 * (SCL_SCAN_B / 32)];
+  constexpr int B = SCL_SCAN_B, NW = B / 32, U = 4;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool inclusive = (flags & 1u) != 0, reverse = (flags & 2u) != 0;
   const scl_T ident = (scl_T)(SCL_IDENTITY);
   const scl_u64 lo = win_rec[4 * r], top = win_rec[4 * r + 1], e0 = win_rec[4 * r + 2];
   const scl_u64 ln = win_rec[4 * r + 3];
   const int len = (int)(ln < (scl_u64)TILE ? ln : (scl_u64)TILE);  // (more only for bad offsets)
   if (len == 0) return;  // (block-uniform) nothing to write for empty vectors
-  auto sx = [](int p) { return p + (p >> 5); };  // staged index
-  for (int k = threadIdx.x; k < TILE / 32; k += B) s_head[k] = 0u;
+  const int shift = scl_stage_aligned<scl_T, TILE, B, 4>(in + e0, len, ts);
   __syncthreads();
-  // heads at logical positions: a vector's first element, or for a reverse
-  // scan its last (logical q <-> physical len - 1 - q)
+  // short vectors: a thread each, in place
   for (scl_u64 sg = lo + threadIdx.x; sg < top; sg += B) {
-    const scl_u64 a = seg_off[sg], b0 = seg_off[sg + 1], b = b0 > a ? b0 : a;
-    if (b == a || a < e0 || b > e0 + (scl_u64)len) continue;
-    const unsigned int q = (unsigned int)(reverse ? e0 + (scl_u64)len - b : a - e0);
-    atomicOr(&s_head[q >> 5], 1u << (q & 31));
-  }
-  for (int p = threadIdx.x; p < len; p += B) ts[sx(p)] = in[e0 + p];
-  __syncthreads();
-  auto head = [&](int q) { return ((s_head[q >> 5] >> (q & 31)) & 1u) != 0; };
-  // each thread folds its chunk of logical positions in place
-  const int q0 = threadIdx.x * C;
-  auto at = [&](int q) { return sx(reverse ? len - 1 - q : q); };
-  scl_T v = ident;
-  bool hd = false;
-  for (int k = 0; k < C; ++k) {
-    const int q = q0 + k;
-    if (q >= len) break;
-    const scl_T x = ts[at(q)];
-    const bool h = head(q);
-    v = h ? x : SCL_FUNC(v, x SCL_OP_ARGS);
-    hd = hd || h;
-    ts[at(q)] = v;
-  }
-  scl_T carry;
-  scl_flag_scan_excl(hd, v, &carry, s_v, s_h SCL_EXTRA_ARGS);
-  // positions before the chunk's first vector start take the earlier chunks' fold
-  for (int k = 0; k < C; ++k) {
-    const int q = q0 + k;
-    if (q >= len || head(q)) break;
-    ts[at(q)] = SCL_FUNC(carry, ts[at(q)] SCL_OP_ARGS);
-  }
-  __syncthreads();
-  for (int p = threadIdx.x; p < len; p += B) {
-    scl_T res;
-    if (inclusive) {
-      res = ts[sx(p)];
-    } else {
-      const int q = reverse ? len - 1 - p : p;
-      res = head(q) ? ident : ts[sx(reverse ? p + 1 : p - 1)];
+    const scl_u64 a = seg_off[sg], b = seg_off[sg + 1];
+    if (b <= a || b - a > SCL_WIN_THREAD || a < e0 || b > e0 + (scl_u64)len) continue;
+    const int nv = (int)(b - a);
+    scl_T* v = ts + (int)(a - e0) + shift;
+    const int step = reverse ? -1 : 1;
+    if (reverse) v += nv - 1;
+    scl_T acc = v[0];
+    if (!inclusive) v[0] = ident;
+#pragma unroll 4
+    for (int e = 1; e < nv; ++e) {
+      const scl_T x = v[e * step];
+      if (inclusive) {
+        acc = SCL_FUNC(acc, x SCL_OP_ARGS);
+        v[e * step] = acc;
+      } else {
+        v[e * step] = acc;
+        acc = SCL_FUNC(acc, x SCL_OP_ARGS);
+      }
     }
-    out[e0 + p] = SCL_EPILOGUE(res);
   }
+  // longer vectors: warp w takes vectors lo + w, lo + w + NW, ... (its next
+  // 32 offset pairs read at once, one per lane)
+  for (scl_u64 g = lo + warp; g < top; g += (scl_u64)NW * 32) {
+    const scl_u64 mine = g + (scl_u64)NW * lane;
+    scl_u64 a_l = 0, b_l = 0;
+    if (mine < top) {
+      a_l = seg_off[mine];
+      b_l = seg_off[mine + 1];
+    }
+    const int cnt = (int)((top - g + NW - 1) / NW < 32 ? (top - g + NW - 1) / NW : 32);
+    for (int k = 0; k < cnt; ++k) {
+      const scl_u64 a = __shfl_sync(0xffffffffu, a_l, k), b = __shfl_sync(0xffffffffu, b_l, k);
+      if (b <= a || b - a <= SCL_WIN_THREAD) continue;  // (empty, or a thread's above)
+      if (a < e0 || b > e0 + (scl_u64)len) continue;  // (only for offsets changed since the plan)
+      const int pa = (int)(a - e0) + shift, nv = (int)(b - a);
+      // logical element e of the vector sits at ts[at(e)]
+      auto at = [&](int e) { return reverse ? pa + nv - 1 - e : pa + e; };
+      scl_T carry = ident;
+      for (int b0 = 0; b0 < nv; b0 += 32 * U) {
+        const int eb = b0 + lane * U;
+        scl_T v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) v[u] = eb + u < nv ? ts[at(eb + u)] : ident;
+#pragma unroll
+        for (int u = 1; u < U; ++u) v[u] = SCL_FUNC(v[u - 1], v[u] SCL_OP_ARGS);
+        const scl_T tot = scl_warp_incl(v[U - 1] SCL_EXTRA_ARGS);
+        scl_T lane_excl = scl_shfl_up(tot, 1);
+        if (lane == 0) lane_excl = ident;
+        const scl_T pre = SCL_FUNC(carry, lane_excl SCL_OP_ARGS);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (eb + u < nv)
+            ts[at(eb + u)] = inclusive ? SCL_FUNC(pre, v[u] SCL_OP_ARGS)
+                                       : (u == 0 ? pre : SCL_FUNC(pre, v[u - 1] SCL_OP_ARGS));
+        }
+        carry = SCL_FUNC(carry, scl_shfl_idx(tot, 31) SCL_OP_ARGS);
+      }
+    }
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < len; p += B) out[e0 + p] = SCL_EPILOGUE(ts[p + shift]);
 }
 
 // The warp-per-segment kernel on its own (segmented launches without a

@@ -116,10 +116,13 @@ def test_first_nonzero_float_in_order(scl, orc, flags):
     assert np.array_equal(dy.to_numpy(), want)
 
 
+@pytest.mark.parametrize("planned", [False, True])
 @pytest.mark.parametrize("flags", FLAGS)
-def test_segmented_affine_in_order(scl, orc, flags):
-    """One ordered scan per segment: short segments (a warp each) and long
-    ones (tiles with a look-back that stops at the segment's first tile)."""
+def test_segmented_affine_in_order(scl, orc, flags, planned):
+    """One ordered scan per segment: short segments (a warp each; with a
+    segment plan, a warp each within a window staged in shared memory) and
+    long ones (tiles with a look-back that stops at the segment's first
+    tile)."""
     rng = np.random.default_rng(5 + flags)
     lens = np.concatenate([rng.integers(0, 300, 2000), rng.integers(5000, 200_000, 20)])
     rng.shuffle(lens)
@@ -129,9 +132,13 @@ def test_segmented_affine_in_order(scl, orc, flags):
     x16 = pack16(x).astype(np.uint32)
     p = S.Program(S.KIND_SCAN, AFFINE16, ["uint"], identity="1u")
     dy = S.DeviceArray(n, np.uint32)
+    doff = S.DeviceArray.from_numpy(off)
+    plan = S.SegPlan(doff, n) if planned else None
     p.launch([S.DeviceArray.from_numpy(x16), dy], n=n, flags=flags,
-             segments=S.DeviceArray.from_numpy(off))
+             segments=plan if planned else doff)
     got = dy.to_numpy()
+    if plan is not None:
+        plan.release()
     inclusive, reverse = flags_of(flags)
     for s in range(len(lens)):
         lo, hi = int(off[s]), int(off[s + 1])
