@@ -383,8 +383,10 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
     void* tickets = pl->tickets;
     void* wseg = cfg->win_rec;
     unsigned int* err = rt().dev_err;
+    unsigned int spin = spin_of(tu);
     ArgPack pack;
-    pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max, &wseg};
+    pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max, &wseg,
+                 &spin};
     if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
       return st;
     const uint64_t grid = cfg->tiles + cfg->n_rec;
@@ -441,8 +443,9 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
     // longer segments: tiles (blocks past the last tile return at once)
     ArgPack pack;
     void* no_windows = nullptr;
+    unsigned int spin = spin_of(tu);
     pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max,
-                 &no_windows};
+                 &no_windows, &spin};
     if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
       return st;
     p->last_variant = SCL_VARIANT_VECTOR;

@@ -331,48 +331,6 @@ struct scl_vec_width {
 // scanned by one thread, a longer one by a warp.
 #define SCL_WIN_THREAD 256
 
-// Copies the 16-byte-aligned vectors covering src[0 .. len) (len <= MAXLEN)
-// to ts as they are, so that src[p] lands at ts[p + shift]; returns shift
-// (the elements of the first vector that lie before src).  CH vectors per
-// thread are in flight before any is stored; ts needs MAXLEN + 16 / sizeof(T)
-// elements and 16-byte alignment.  The first and last vectors may hold
-// elements outside the range (an aligned 16-byte vector lies within one page
-// of the buffer that holds its in-range elements).  Elements that do not
-// tile 16 bytes, or do not sit on their own size, are copied one by one
-// (shift 0).
-template <typename T, int MAXLEN, int B, int CH>
-__device__ __forceinline__ int scl_stage_aligned(const T* src, int len, T* ts) {
-  constexpr int V = scl_vec_width<sizeof(T)>::value;
-  const unsigned long long addr = (unsigned long long)src;
-  if constexpr (V == 1) {
-    for (int p = threadIdx.x; p < len; p += B) ts[p] = src[p];
-    return 0;
-  }
-  if (addr % sizeof(T) != 0) {
-    for (int p = threadIdx.x; p < len; p += B) ts[p] = src[p];
-    return 0;
-  }
-  const int mis = (int)((addr & 15u) / sizeof(T));
-  const T* base = src - mis;
-  const int nv = len > 0 ? (mis + len + V - 1) / V : 0;
-  constexpr int PER = (MAXLEN + V - 1) / V / B + 1;  // vectors per thread at most
-#pragma unroll
-  for (int k0 = 0; k0 < PER; k0 += CH) {
-    scl_pack<T, V> buf[CH];
-#pragma unroll
-    for (int k = 0; k < CH; ++k) {
-      const int v = threadIdx.x + (k0 + k) * B;
-      if (k0 + k < PER && v < nv) buf[k] = scl_load<T, V>(base + (scl_u64)v * V);
-    }
-#pragma unroll
-    for (int k = 0; k < CH; ++k) {
-      const int v = threadIdx.x + (k0 + k) * B;
-      if (k0 + k < PER && v < nv) scl_store<T, V>(ts + v * V, buf[k]);
-    }
-  }
-  return mis;
-}
-
 // Device-side status word: bit 0 = a bounded wait gave up.
 #define SCL_DEV_ERR_TIMEOUT 1u
 __device__ __forceinline__ void scl_raise(unsigned int* err, unsigned int bit) {
@@ -380,6 +338,73 @@ __device__ __forceinline__ void scl_raise(unsigned int* err, unsigned int bit) {
 }
 __device__ __forceinline__ void scl_nanosleep(unsigned int ns) {
   asm volatile("nanosleep.u32 %0;" :: "r"(ns));
+}
+
+// Bounded wait for phase 0 of the mbarrier at shared address bar_s: false
+// after spin_limit polls without completion.
+__device__ __forceinline__ bool scl_mbar_wait(unsigned int bar_s, unsigned int spin_limit) {
+  unsigned int done = 0, polls = 0;
+  while (!done) {
+    asm volatile(
+        "{ .reg .pred p; mbarrier.test_wait.parity.shared::cta.b64 p, [%1], 0;"
+        " selp.u32 %0, 1, 0, p; }"
+        : "=r"(done) : "r"(bar_s) : "memory");
+    if (!done) {
+      if (++polls > spin_limit) return false;
+      if (polls > 16) scl_nanosleep(32);
+    }
+  }
+  return true;
+}
+
+// Starts bringing src[0 .. len) (len <= MAXLEN) into shared memory so that
+// src[p] lands at ts[p + shift]; returns shift, the elements between src
+// and the 16-byte boundary below it, so that 16-byte-aligned global addresses
+// meet 16-byte-aligned shared ones.  The 16-byte-aligned interior of the
+// range goes by bulk asynchronous copies that thread 0 issues on the
+// mbarrier bar_s (initialised by the caller, phase 0); *tx receives the bytes
+// it counts (0: nothing issued, no wait needed).  The ragged ends (under 16
+// bytes each) are read by ordinary loads of the calling threads, so nothing
+// outside the range is read.  Elements that do not tile 16 bytes, or do not
+// sit on their own size, are all read by ordinary loads (shift 0).  The
+// caller waits on the mbarrier (thread 0) and then synchronises the block.
+template <typename T, int MAXLEN, int B>
+__device__ __forceinline__ int scl_stage_bulk(const T* src, int len, T* ts, unsigned int bar_s,
+                                              unsigned int* tx) {
+  constexpr int V = scl_vec_width<sizeof(T)>::value;
+  *tx = 0u;
+  const unsigned long long addr = (unsigned long long)src;
+  if (V == 1 || addr % sizeof(T) != 0 || len <= 0) {
+    for (int p = threadIdx.x; p < len; p += B) ts[p] = src[p];
+    return 0;
+  }
+  const int shift = (int)((addr & 15u) / sizeof(T));
+  const int head = shift ? V - shift : 0;  // elements before the first boundary
+  const int lo = head < len ? head : len;
+  const int hi_raw = (shift + len) / V * V - shift;  // end of the aligned interior
+  const int hi = hi_raw > lo ? hi_raw : lo;
+  if (hi > lo) {
+    const unsigned int bytes = (unsigned int)((hi - lo) * (int)sizeof(T));
+    *tx = bytes;
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                   :: "r"(bar_s), "r"(bytes) : "memory");
+      const unsigned int dst = (unsigned int)__cvta_generic_to_shared(ts + lo + shift);
+      constexpr unsigned int CHUNK = 8192;  // bytes per copy
+      for (unsigned int o = 0; o < bytes; o += CHUNK) {
+        const unsigned int sz = bytes - o < CHUNK ? bytes - o : CHUNK;
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+            :: "r"(dst + o), "l"((const void*)((const char*)(src + lo) + o)), "r"(sz), "r"(bar_s)
+            : "memory");
+      }
+    }
+  }
+  // the ragged ends
+  const int ntail = len - hi;
+  if ((int)threadIdx.x < lo) ts[threadIdx.x + shift] = src[threadIdx.x];
+  if ((int)threadIdx.x < ntail) ts[hi + threadIdx.x + shift] = src[hi + threadIdx.x];
+  return shift;
 }
 __device__ __forceinline__ unsigned int scl_ld_acquire(const unsigned int* p) {
   unsigned int v;

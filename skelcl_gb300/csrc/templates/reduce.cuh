@@ -268,30 +268,60 @@ scl_reduce_short(const scl_T* in, scl_T* out, const scl_u64* seg_off, scl_u64 n_
 // first element, elements}: consecutive vectors of at most short_max elements
 // that start in one window of short_max elements (all but the last end
 // inside it, so the record spans at most 2 * short_max = WT elements).  The
-// 16-byte vectors covering the record's elements are copied to shared memory
-// as they are (element e0 + p at ts[p + shift]).  Then a vector of at most
-// SCL_WIN_THREAD elements is folded by one thread (four interleaved folds of
-// the elements e = 0, 1, 2, 3 mod 4, combined at the end; in element order
-// below 8 elements); a longer one by a warp: lane l folds elements l, l + 32, ... in order and the
-// lanes' folds combine in a shuffle tree (a strided fold and a tree, as in
-// the flat reduce; the operator is taken to be commutative), each warp
-// reading the offsets of its next 32 vectors at once.  An empty vector
+// record's elements are brought into shared memory by bulk asynchronous
+// copies (element e0 + p at ts[p + shift]; bounded wait) while each thread
+// reads its first vector's offsets.  Then a vector of at most SCL_WIN_THREAD
+// elements is folded by one thread (four interleaved folds of the elements
+// e = 0, 1, 2, 3 mod 4, combined at the end; in element order below 8
+// elements), a longer one by a warp: lane l folds elements l, l + 32, ... in
+// order and the lanes' folds combine in a shuffle tree (a strided fold and a
+// tree, as in the flat reduce; the operator is taken to be commutative), each
+// warp reading the offsets of its next 32 vectors at once.  An empty vector
 // yields SCL_IDENTITY.  Folds in the element type.
 template <int WT>
 __device__ __forceinline__ void scl_reduce_window_run(const scl_T* in, scl_T* out, const scl_u64* seg_off,
-                                                      const scl_u64* win_rec, scl_u64 r,
-                                                      scl_T* ts SCL_USER_PARAMS) {
+                                                      const scl_u64* win_rec, scl_u64 r, scl_T* ts,
+                                                      unsigned int spin_limit,
+                                                      unsigned int* err SCL_USER_PARAMS) {
   constexpr int B = 256, NW = B / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const scl_T ident = (scl_T)(SCL_IDENTITY);
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ int s_ok;
+  const unsigned int bar_s = (unsigned int)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar_s));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
   const scl_u64 lo = win_rec[4 * r], top = win_rec[4 * r + 1], e0 = win_rec[4 * r + 2];
   const scl_u64 ln = win_rec[4 * r + 3];
   const int len = (int)(ln < (scl_u64)WT ? ln : (scl_u64)WT);  // (more only for bad offsets)
-  const int shift = scl_stage_aligned<scl_T, WT, B, 4>(in + e0, len, ts);
+  unsigned int tx;
+  const int shift = scl_stage_bulk<scl_T, WT, B>(in + e0, len, ts, bar_s, &tx);
+  // this thread's first vector's offsets are read while the copy lands
+  scl_u64 sg = lo + threadIdx.x;
+  scl_u64 a_n = 0, b_n = 0;
+  if (sg < top) {
+    a_n = seg_off[sg];
+    b_n = seg_off[sg + 1];
+  }
+  if (threadIdx.x == 0) {
+    bool ok = tx == 0u || scl_mbar_wait(bar_s, spin_limit);
+    if (!ok) {
+      scl_raise(err, SCL_DEV_ERR_TIMEOUT);
+      scl_mbar_wait(bar_s, 1u << 21);  // the copy may still land here: stay (bounded) until it has
+    }
+    s_ok = ok ? 1 : 0;
+  }
   __syncthreads();
+  if (!s_ok) return;
   // short vectors (and empty ones): a thread each
-  for (scl_u64 sg = lo + threadIdx.x; sg < top; sg += B) {
-    const scl_u64 a = seg_off[sg], b0 = seg_off[sg + 1], b = b0 > a ? b0 : a;
+  for (; sg < top; sg += B) {
+    const scl_u64 a = a_n, b0 = b_n, b = b0 > a ? b0 : a;
+    if (sg + B < top) {
+      a_n = seg_off[sg + B];
+      b_n = seg_off[sg + B + 1];
+    }
     if (b == a) {
       out[sg] = ident;
       continue;
@@ -365,16 +395,17 @@ __global__ void __launch_bounds__(256)
 scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
                const unsigned int* tile_start, scl_u64 n_seg, int aligned, scl_C* partials,
                unsigned int* tickets, unsigned int* err, scl_u64 short_max,
-               const scl_u64* win_rec SCL_EXTRA_PARAMS) {
+               const scl_u64* win_rec, unsigned int spin_limit SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
   (void)short_max;
   (void)win_rec;
+  (void)spin_limit;
   if constexpr (MERGED != 0) {
     const unsigned int nt = tile_start[n_seg];
     if (blockIdx.x >= nt) {  // (block-uniform: the whole block takes the window role)
       constexpr int WT = 8 * 256 * scl_vec_width<sizeof(scl_T)>::value;  // 32 KB of elements
       scl_reduce_window_run<WT>(in, out, seg_off, win_rec, blockIdx.x - nt,
-                                reinterpret_cast<scl_T*>(scl_dyn_smem) SCL_EXTRA_ARGS);
+                                reinterpret_cast<scl_T*>(scl_dyn_smem), spin_limit, err SCL_EXTRA_ARGS);
       return;
     }
   }

@@ -374,20 +374,6 @@ scl_scan_k(const scl_T* in, scl_T* out, scl_u64 n, unsigned int flags, int align
 // as many as the register file allows with the tile in registers (4).
 // Reverse, ragged and unaligned tiles are staged with ordinary loads.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool scl_mbar_wait(unsigned int bar_s, unsigned int spin_limit) {
-  unsigned int done = 0, polls = 0;
-  while (!done) {
-    asm volatile(
-        "{ .reg .pred p; mbarrier.test_wait.parity.shared::cta.b64 p, [%1], 0;"
-        " selp.u32 %0, 1, 0, p; }"
-        : "=r"(done) : "r"(bar_s) : "memory");
-    if (!done) {
-      if (++polls > spin_limit) return false;
-      if (polls > 16) scl_nanosleep(32);
-    }
-  }
-  return true;
-}
 
 // Segmented scan of the segments of at most short_max elements: one warp per
 // segment, warps striding over the segments (warp `wid` of `nw`); per round
@@ -477,9 +463,10 @@ __device__ __forceinline__ void scl_scan_short_run(const scl_T* in, scl_O* out, 
 // element, elements}: consecutive vectors of at most short_max elements that
 // start in one window of short_max elements (all but the last end inside
 // it, so the record spans at most 2 * short_max = TILE elements, one staged
-// tile).  The 16-byte vectors covering the record's elements are copied to
-// shared memory as they are (element e0 + p at ts[p + shift]) and every
-// vector is scanned in place there: one of at most SCL_WIN_THREAD elements by
+// tile).  The record's elements are brought into shared memory by bulk
+// asynchronous copies (element e0 + p at ts[p + shift]; bounded wait) while
+// each thread reads its first vector's offsets, and every vector is scanned
+// in place there: one of at most SCL_WIN_THREAD elements by
 // one thread, in element order; a longer one by a warp, in rounds of 32 x U
 // logical elements (lane l holds U consecutive ones; a reverse scan reads the
 // vector from its end), the lanes' totals scanned across the warp and rounds
@@ -490,7 +477,9 @@ __device__ __forceinline__ void scl_scan_short_run(const scl_T* in, scl_O* out, 
 template <int TILE>
 __device__ __forceinline__ void scl_scan_window_run(const scl_T* in, scl_O* out, const scl_u64* seg_off,
                                                     const scl_u64* win_rec, scl_u64 r,
-                                                    unsigned int flags, scl_T* ts SCL_USER_PARAMS) {
+                                                    unsigned int flags, scl_T* ts, unsigned int bar_s,
+                                                    unsigned int spin_limit,
+                                                    unsigned int* err SCL_USER_PARAMS) {
   constexpr int B = SCL_SCAN_B, NW = B / 32, U = 4;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool inclusive = (flags & 1u) != 0, reverse = (flags & 2u) != 0;
@@ -499,11 +488,33 @@ __device__ __forceinline__ void scl_scan_window_run(const scl_T* in, scl_O* out,
   const scl_u64 ln = win_rec[4 * r + 3];
   const int len = (int)(ln < (scl_u64)TILE ? ln : (scl_u64)TILE);  // (more only for bad offsets)
   if (len == 0) return;  // (block-uniform) nothing to write for empty vectors
-  const int shift = scl_stage_aligned<scl_T, TILE, B, 4>(in + e0, len, ts);
+  __shared__ int s_ok;
+  unsigned int tx;
+  const int shift = scl_stage_bulk<scl_T, TILE, B>(in + e0, len, ts, bar_s, &tx);
+  // this thread's first vector's offsets are read while the copy lands
+  scl_u64 sg = lo + threadIdx.x;
+  scl_u64 a_n = 0, b_n = 0;
+  if (sg < top) {
+    a_n = seg_off[sg];
+    b_n = seg_off[sg + 1];
+  }
+  if (threadIdx.x == 0) {
+    bool ok = tx == 0u || scl_mbar_wait(bar_s, spin_limit);
+    if (!ok) {
+      scl_raise(err, SCL_DEV_ERR_TIMEOUT);
+      scl_mbar_wait(bar_s, 1u << 21);  // the copy may still land here: stay (bounded) until it has
+    }
+    s_ok = ok ? 1 : 0;
+  }
   __syncthreads();
+  if (!s_ok) return;
   // short vectors: a thread each, in place
-  for (scl_u64 sg = lo + threadIdx.x; sg < top; sg += B) {
-    const scl_u64 a = seg_off[sg], b = seg_off[sg + 1];
+  for (; sg < top; sg += B) {
+    const scl_u64 a = a_n, b = b_n;
+    if (sg + B < top) {
+      a_n = seg_off[sg + B];
+      b_n = seg_off[sg + B + 1];
+    }
     if (b <= a || b - a > SCL_WIN_THREAD || a < e0 || b > e0 + (scl_u64)len) continue;
     const int nv = (int)(b - a);
     scl_T* v = ts + (int)(a - e0) + shift;
@@ -639,7 +650,8 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
   if constexpr (SEG == 2) {
     const unsigned int nt = tile_start[n_seg];
     if (blockIdx.x >= nt) {  // (block-uniform: the whole block takes the window role)
-      scl_scan_window_run<TILE>(in, out, seg_off, win_rec, blockIdx.x - nt, flags, ts SCL_EXTRA_ARGS);
+      scl_scan_window_run<TILE>(in, out, seg_off, win_rec, blockIdx.x - nt, flags, ts, bar_s, spin_limit,
+                                err SCL_EXTRA_ARGS);
       return;
     }
   }
