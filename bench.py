@@ -720,6 +720,16 @@ def segmented_short(S, oracle, hbm_peak):
     ref = np.array([oracle.sum_f64(x[int(off[i]):int(off[i + 1])]) for i in pick])
     flat_scan = timed(S, lambda: sp.launch([dx, dy], n=n, flags=S.SHAPE_INCLUSIVE), 10, 3)
     flat_red = timed(S, lambda: rp.launch([dx, dr], n=n), 10, 3)
+    # the adjoint of the segmented Reduce: each vector's gradient broadcast
+    # over its elements, against the flat broadcast of one value
+    L = S.lib()
+    seg_bc = timed(S, lambda: S.check(L.scl_adjoint_broadcast_segments(dr.ptr, dy.ptr, doff.ptr, nseg, n,
+                                                                       S.DTYPE_F32, 0)), 10, 3)
+    flat_bc = timed(S, lambda: S.check(L.scl_adjoint_broadcast(dr.ptr, dy.ptr, n, S.DTYPE_F32, 0)), 10, 3)
+    S.check(L.scl_adjoint_broadcast_segments(dr.ptr, dy.ptr, doff.ptr, nseg, n, S.DTYPE_F32, 0))
+    gb = dy.to_numpy()
+    ids = np.repeat(np.arange(nseg), lens.astype(np.int64))
+    bc_ok = bool(np.array_equal(gb, dr.to_numpy()[ids]))
     plan.release()
     return {"n_vectors": nseg, "elements": n,
             "scan": {"ms": round(seg_scan, 4), "GBps": round(8 * n / seg_scan / 1e6, 1),
@@ -727,6 +737,8 @@ def segmented_short(S, oracle, hbm_peak):
             "reduce": {"ms": round(seg_red, 4), "GBps": round(4 * n / seg_red / 1e6, 1),
                        "flat_ms": round(flat_red, 4), "without_plan_ms": round(np_red, 4),
                        "max_abs_err_vs_fp64_sampled": float(np.abs(sums[pick] - ref).max())},
+            "broadcast_adjoint": {"ms": round(seg_bc, 4), "GBps": round(4 * n / seg_bc / 1e6, 1),
+                                  "flat_ms": round(flat_bc, 4), "exact": bc_ok},
             "note": "with a segment plan: one launch per call, the short vectors in window records "
                     "staged in shared memory; without it the offsets pre-pass runs on every call and "
                     "each short vector takes a warp"}

@@ -164,61 +164,88 @@ seg_tile_start_kernel(const uint64_t* off, uint64_t n_seg, uint64_t tile, uint64
 }
 
 // gx[i] (+)= g[s] for every element i of segment s (elements outside every
-// segment are left alone).  Each block takes a chunk of CH elements; its
-// threads walk the offsets forward from the chunk's first segment.  With a
-// 16-byte aligned gx, a vector of 16 bytes inside one segment is written with
-// one store.
+// segment are left alone).  Each warp takes a chunk of CH elements: it finds
+// the last segment starting at or before the chunk (a search of the warp, 32
+// probes per round), then walks the segments that start before the chunk's
+// end, the offsets and values of 32 of them read at once, and writes each
+// one's part of the chunk with lane-strided stores (16 bytes at a time when
+// gx is 16-byte aligned, single elements at the part's ragged ends).
 template <typename T>
-__global__ void broadcast_segments_kernel(const T* __restrict__ g, T* __restrict__ gx,
-                                          const uint64_t* __restrict__ off, uint64_t n_seg,
-                                          uint64_t n_total, int acc, int aligned) {
-  constexpr int CH = 8192, V = 16 / sizeof(T);
-  const uint64_t c0 = (uint64_t)blockIdx.x * CH;
+__global__ void __launch_bounds__(256)
+broadcast_segments_kernel(const T* __restrict__ g, T* __restrict__ gx, const uint64_t* __restrict__ off,
+                          uint64_t n_seg, uint64_t n_total, int acc, int aligned) {
+  constexpr int CH = 1024, V = 16 / sizeof(T);
+  const int lane = threadIdx.x & 31;
+  const uint64_t c0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * CH;
+  if (c0 >= n_total) return;  // (warp-uniform)
   const uint64_t c1 = c0 + CH < n_total ? c0 + CH : n_total;
-  __shared__ uint64_t s_first;
-  if (threadIdx.x == 0) {
-    // last segment s with off[s] <= c0 (0 if none)
-    uint64_t lo = 0, hi = n_seg - 1;
-    while (lo < hi) {
-      const uint64_t mid = (lo + hi + 1) / 2;
-      if (off[mid] <= c0) lo = mid; else hi = mid - 1;
+  // last segment with off[s] <= c0 (0 if none): each round the lanes probe 32
+  // offsets spread over [lo, hi] and the count at or below c0 narrows it (by
+  // 32 for increasing offsets; decreasing ones still end the search)
+  uint64_t lo = 0, hi = n_seg - 1;
+  while (lo < hi) {  // (warp-uniform)
+    const uint64_t span = hi - lo;
+    const uint64_t p = lo + 1 + span * (uint64_t)lane / 32;
+    const int below = __popc(__ballot_sync(0xffffffffu, off[p] <= c0));
+    if (below == 0) {
+      hi = lo;
+    } else {
+      const uint64_t p_last = lo + 1 + span * (uint64_t)(below - 1) / 32;
+      hi = below < 32 ? lo + span * (uint64_t)below / 32 : hi;
+      lo = p_last;
     }
-    s_first = lo;
   }
-  __syncthreads();
-  uint64_t s = s_first;
-  auto one = [&](uint64_t i) {
-    while (s + 1 < n_seg && i >= off[s + 1]) ++s;
-    if (i < off[s] || i >= off[s + 1]) return;
-    const T v = g[s];
-    gx[i] = acc ? gx[i] + v : v;
-  };
-  if (!aligned) {
-    for (uint64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) one(i);
-    return;
-  }
-  for (uint64_t i = c0 + (uint64_t)threadIdx.x * V; i < c1; i += (uint64_t)blockDim.x * V) {
-    while (s + 1 < n_seg && i >= off[s + 1]) ++s;
-    if (i + V <= c1 && i >= off[s] && i + V <= off[s + 1]) {
-      const T v = g[s];
+  auto one = [&](uint64_t i, T v) { gx[i] = acc ? gx[i] + v : v; };
+  // this warp's part [i0, i1) of one segment, value v
+  auto put = [&](uint64_t i0, uint64_t i1, T v) {
+    if (!aligned) {
+      for (uint64_t i = i0 + lane; i < i1; i += 32) one(i, v);
+      return;
+    }
+    const uint64_t h0 = (i0 + V - 1) / V * V;
+    const uint64_t h = h0 < i1 ? h0 : i1;            // end of the ragged head
+    const uint64_t t0 = i1 / V * V, t = t0 > h ? t0 : h;  // start of the ragged tail
+    if (i0 + lane < h) one(i0 + lane, v);
+    for (uint64_t q = h + (uint64_t)lane * V; q < t; q += 32 * V) {
       T r[V];
       if (acc) {
-        const uint4 q = *reinterpret_cast<const uint4*>(gx + i);
-        memcpy(r, &q, 16);
+        const uint4 w = *reinterpret_cast<const uint4*>(gx + q);
+        memcpy(r, &w, 16);
 #pragma unroll
         for (int e = 0; e < V; ++e) r[e] += v;
       } else {
 #pragma unroll
         for (int e = 0; e < V; ++e) r[e] = v;
       }
-      uint4 q;
-      memcpy(&q, r, 16);
-      *reinterpret_cast<uint4*>(gx + i) = q;
-    } else {
-      const uint64_t s_keep = s;
-      for (int e = 0; e < V && i + e < c1; ++e) one(i + e);
-      s = s_keep;
+      uint4 w;
+      memcpy(&w, r, 16);
+      *reinterpret_cast<uint4*>(gx + q) = w;
     }
+    if (t + lane < i1) one(t + lane, v);
+  };
+  for (uint64_t sb = lo; sb < n_seg; sb += 32) {
+    const uint64_t my = sb + lane;
+    uint64_t a_l = n_total, b_l = n_total;
+    T v_l = T(0);
+    if (my < n_seg) {
+      a_l = off[my];
+      b_l = off[my + 1];
+      v_l = g[my];
+    }
+    const int cnt = n_seg - sb < 32 ? (int)(n_seg - sb) : 32;
+    bool past = false;
+    for (int k = 0; k < cnt; ++k) {
+      const uint64_t a = __shfl_sync(0xffffffffu, a_l, k), b0 = __shfl_sync(0xffffffffu, b_l, k);
+      const T v = __shfl_sync(0xffffffffu, v_l, k);
+      if (a >= c1) {  // this and (for increasing offsets) every later segment start past the chunk
+        past = true;
+        break;
+      }
+      const uint64_t b = b0 > a ? b0 : a;
+      const uint64_t i0 = a > c0 ? a : c0, i1 = b < c1 ? b : c1;
+      if (i0 < i1) put(i0, i1, v);
+    }
+    if (past) break;
   }
 }
 
@@ -412,7 +439,7 @@ extern "C" int scl_adjoint_broadcast_segments(const void* g, void* gx, const uin
     return fail(SCL_ERR_ARG, "segmented broadcast: dtype must be SCL_DTYPE_F32 or _F64");
   if (n == 0 || n_segments == 0) return SCL_OK;
   if (!g || !gx || !seg_offsets) return fail(SCL_ERR_ARG, "segmented broadcast: null pointer");
-  const uint64_t blocks = (n + 8191) / 8192;
+  const uint64_t blocks = (n + 8191) / 8192;  // 8 warps of 1024 elements each
   if (blocks > 0x7fffffffull) return fail(SCL_ERR_ARG, "segmented broadcast: vector too large");
   const int acc = accumulate ? 1 : 0;
   const int aligned = (reinterpret_cast<uintptr_t>(gx) & 15u) == 0 ? 1 : 0;
