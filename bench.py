@@ -910,7 +910,8 @@ def run_case(args):
         nbytes = 8 * n
     elif c == "segmented_short":
         # n vectors of 1..199 float elements (uniform, seed 1), values
-        # U[-1,1] (seed 2): a segmented inclusive Scan(+) and Reduce(+) per step
+        # U[-1,1] (seed 2): a segmented inclusive Scan(+) and Reduce(+) per
+        # step, and the Reduce's adjoint (each vector's value broadcast)
         rng = np.random.default_rng(1)
         lens = rng.integers(1, 200, n).astype(np.uint64)
         off = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
@@ -922,10 +923,13 @@ def run_case(args):
 
         plan = S.SegPlan(doff, ne)
 
+        L = S.lib()
+
         def fn():
             sp.launch([a, z], n=ne, flags=S.SHAPE_INCLUSIVE, segments=plan)
             rp.launch([a, r], n=ne, segments=plan)
-        nbytes = 12 * ne
+            S.check(L.scl_adjoint_broadcast_segments(r.ptr, z.ptr, doff.ptr, n, ne, S.DTYPE_F32, 0))
+        nbytes = 16 * ne
     elif c in ("zip_mul", "reduce_f32", "scan_f32"):
         a = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 0, -1.0, 1.0))
         b = S.DeviceArray.from_numpy(oracle.uniform_f32(n, 1, -1.0, 1.0))

@@ -195,21 +195,23 @@ broadcast_segments_kernel(const T* __restrict__ g, T* __restrict__ gx, const uin
       lo = p_last;
     }
   }
-  auto one = [&](uint64_t i, T v) { gx[i] = acc ? gx[i] + v : v; };
-  // this warp's part [i0, i1) of one segment, value v
-  auto put = [&](uint64_t i0, uint64_t i1, T v) {
+  // this warp's part [r0, r1) of one segment, value v, as offsets from c0
+  // (a multiple of CH, so offsets and indices share their 16-byte phase)
+  T* const base = gx + c0;
+  auto one = [&](int r, T v) { base[r] = acc ? base[r] + v : v; };
+  auto put = [&](int r0, int r1, T v) {
     if (!aligned) {
-      for (uint64_t i = i0 + lane; i < i1; i += 32) one(i, v);
+      for (int r = r0 + lane; r < r1; r += 32) one(r, v);
       return;
     }
-    const uint64_t h0 = (i0 + V - 1) / V * V;
-    const uint64_t h = h0 < i1 ? h0 : i1;            // end of the ragged head
-    const uint64_t t0 = i1 / V * V, t = t0 > h ? t0 : h;  // start of the ragged tail
-    if (i0 + lane < h) one(i0 + lane, v);
-    for (uint64_t q = h + (uint64_t)lane * V; q < t; q += 32 * V) {
+    const int h0 = (r0 + V - 1) & ~(V - 1);
+    const int h = h0 < r1 ? h0 : r1;                        // end of the ragged head
+    const int t0 = r1 & ~(V - 1), t = t0 > h ? t0 : h;      // start of the ragged tail
+    if (r0 + lane < h) one(r0 + lane, v);
+    for (int q = h + lane * V; q < t; q += 32 * V) {
       T r[V];
       if (acc) {
-        const uint4 w = *reinterpret_cast<const uint4*>(gx + q);
+        const uint4 w = *reinterpret_cast<const uint4*>(base + q);
         memcpy(r, &w, 16);
 #pragma unroll
         for (int e = 0; e < V; ++e) r[e] += v;
@@ -219,9 +221,9 @@ broadcast_segments_kernel(const T* __restrict__ g, T* __restrict__ gx, const uin
       }
       uint4 w;
       memcpy(&w, r, 16);
-      *reinterpret_cast<uint4*>(gx + q) = w;
+      *reinterpret_cast<uint4*>(base + q) = w;
     }
-    if (t + lane < i1) one(t + lane, v);
+    if (t + lane < r1) one(t + lane, v);
   };
   for (uint64_t sb = lo; sb < n_seg; sb += 32) {
     const uint64_t my = sb + lane;
@@ -243,7 +245,7 @@ broadcast_segments_kernel(const T* __restrict__ g, T* __restrict__ gx, const uin
       }
       const uint64_t b = b0 > a ? b0 : a;
       const uint64_t i0 = a > c0 ? a : c0, i1 = b < c1 ? b : c1;
-      if (i0 < i1) put(i0, i1, v);
+      if (i0 < i1) put((int)(i0 - c0), (int)(i1 - c0), v);
     }
     if (past) break;
   }
