@@ -523,7 +523,8 @@ def secondary(S, oracle, hbm_peak, args):
         "fwd_plus_adjoint_over_fwd": round((fwd + bwd) / fwd, 3),
         "max_abs_err_vs_fp64": float(np.abs(yf - ref).max()),
         "max_abs_prefix": float(np.abs(ref).max()),
-        "note": "about 13 us per call is fixed (launch, ramp of the first wave's look-back): 2^28 below"}
+        "note": "about 10 us per call is fixed (launch, ramp of the first wave's look-back), and the FP64 "
+                "carries cost about 3 % (104 against 101 us at 2^26 with float carries): 2^28 below"}
     del dxf, dg, dyf, dgx, yf, ref
     n4 = 1 << 28
     hx4 = oracle.uniform_f32(n4, 2, -1.0, 1.0)
@@ -739,9 +740,9 @@ def segmented_short(S, oracle, hbm_peak):
                        "max_abs_err_vs_fp64_sampled": float(np.abs(sums[pick] - ref).max())},
             "broadcast_adjoint": {"ms": round(seg_bc, 4), "GBps": round(4 * n / seg_bc / 1e6, 1),
                                   "flat_ms": round(flat_bc, 4), "exact": bc_ok},
-            "note": "with a segment plan: one launch per call, the short vectors in window records "
-                    "staged in shared memory; without it the offsets pre-pass runs on every call and "
-                    "each short vector takes a warp"}
+            "note": "with a segment plan: one launch per call, the short vectors' window records "
+                    "bulk-copied into shared memory, a thread per vector of up to 256 elements; without "
+                    "it the offsets pre-pass runs on every call and each short vector takes a warp"}
 
 
 def segmented(S, oracle, hbm_peak):
