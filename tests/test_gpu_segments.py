@@ -209,6 +209,32 @@ def test_segmented_broadcast(scl, dtype, code):
     assert np.array_equal(gx.to_numpy(), (g[ids] + dtype(0.5)).astype(dtype))
 
 
+@pytest.mark.parametrize("shift", [1, 3])
+@pytest.mark.parametrize("accumulate", [0, 1])
+def test_segmented_broadcast_unaligned_and_short(scl, shift, accumulate):
+    """The broadcast on a gx that does not start on 16 bytes (element-wise
+    stores), over many short vectors, empty ones, vectors that start before
+    or reach past a warp's 1024-element chunk, and elements before the first
+    vector and after the last (left alone)."""
+    rng = np.random.default_rng(20 + shift)
+    lens = np.concatenate([rng.integers(0, 40, 5000), [0, 1, 1023, 1024, 1025, 5000, 0]])
+    rng.shuffle(lens)
+    lead, tail = 37, 11
+    off = (lead + np.concatenate([[0], np.cumsum(lens)])).astype(np.uint64)
+    n = int(off[-1]) + tail
+    g = rng.uniform(-1, 1, len(lens)).astype(np.float32)
+    base = rng.uniform(-1, 1, n + shift).astype(np.float32)
+    dbase, dg, doff = dev(base), dev(g), dev(off)
+    gx = dbase.view(shift, n)
+    S.check(S.lib().scl_adjoint_broadcast_segments(dg.ptr, gx.ptr, doff.ptr, len(lens), n, S.DTYPE_F32,
+                                                   accumulate))
+    want = base[shift:].copy()
+    ids = np.repeat(np.arange(len(lens)), lens)
+    sl = slice(lead, lead + int(lens.sum()))
+    want[sl] = (want[sl] + g[ids]).astype(np.float32) if accumulate else g[ids]
+    assert np.array_equal(gx.to_numpy(), want)
+
+
 def test_segmented_pipeline_in_a_graph(scl, orc):
     """Map(x*x+1) -> segmented inclusive Scan -> segmented Reduce, replayed from
     a captured CUDA graph after one eager run (which sizes the workspaces)."""

@@ -72,3 +72,55 @@ def test_reduce_scan_types(scl, dtype):
             res = incl if flags & S.SHAPE_INCLUSIVE else incl - v.astype(acc)
             res = res[::-1] if flags & S.SHAPE_REVERSE else res
             assert close(ds.to_numpy(), res.astype(dtype), dtype, n), (n, flags)
+
+
+@pytest.mark.parametrize("dtype", TYPES, ids=lambda t: np.dtype(t).name)
+def test_planned_segments_types_and_unaligned_views(scl, dtype):
+    """Segmented Scan (all four forms) and Reduce with a segment plan over
+    every element type, on views that start 0..3 elements past a 16-byte
+    boundary: the window records' bulk-copied interiors and plain-loaded ends
+    at every phase, vectors of one thread (<= 256 elements), of a warp and of
+    the tiles, and empty ones."""
+    t = S.CL_TYPE[np.dtype(dtype)]
+    src = f"{t} func({t} x, {t} y){{ return x + y; }}"
+    sp = S.Program(S.KIND_SCAN, src, [t], identity="0")
+    rp = S.Program(S.KIND_REDUCE, src, [t], identity="0")
+    rng = np.random.default_rng(40)
+    lens = np.concatenate([rng.integers(0, 260, 3000), rng.integers(257, 4096, 60),
+                           rng.integers(4097, 20_000, 4), [0, 1, 255, 256, 257, 4096, 0]])
+    rng.shuffle(lens)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+    n = int(off[-1])
+    ids = np.repeat(np.arange(len(lens)), lens)
+    doff = dev(off)
+    for shift in range(4):
+        x = data(dtype, n + shift, 41 + shift)
+        base = dev(x)
+        dx = base.view(shift, n)
+        xs = x[shift:]
+        dy, dr = S.DeviceArray(n, dtype), S.DeviceArray(len(lens), dtype)
+        plan = S.SegPlan(doff, n)
+        try:
+            for flags in (0, 1, 2, 3):
+                sp.launch([dx, dy], n=n, flags=flags, segments=plan)
+                got = dy.to_numpy()
+                inclusive, reverse = bool(flags & 1), bool(flags & 2)
+                want = np.empty(n, dtype)
+                for s in range(len(lens)):
+                    lo, hi = int(off[s]), int(off[s + 1])
+                    if lo == hi:
+                        continue
+                    seg = xs[lo:hi][::-1] if reverse else xs[lo:hi]
+                    with np.errstate(over="ignore"):
+                        c = np.cumsum(seg, dtype=dtype)
+                        if not inclusive:
+                            c = np.concatenate([[dtype(0)], c[:-1]]).astype(dtype)
+                    want[lo:hi] = c[::-1] if reverse else c
+                assert close(got, want, dtype, terms=int(lens.max())), (shift, flags)
+            rp.launch([dx, dr], n=n, segments=plan)
+            with np.errstate(over="ignore"):
+                sums = np.zeros(len(lens), dtype)
+                np.add.at(sums, ids, xs)
+            assert close(dr.to_numpy(), sums, dtype, terms=int(lens.max())), (shift, "reduce")
+        finally:
+            plan.release()
