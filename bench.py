@@ -523,8 +523,8 @@ def secondary(S, oracle, hbm_peak, args):
         "fwd_plus_adjoint_over_fwd": round((fwd + bwd) / fwd, 3),
         "max_abs_err_vs_fp64": float(np.abs(yf - ref).max()),
         "max_abs_prefix": float(np.abs(ref).max()),
-        "note": "about 10 us per call is fixed (launch, ramp of the first wave's look-back), and the FP64 "
-                "carries cost about 3 % (104 against 101 us at 2^26 with float carries): 2^28 below"}
+        "note": "about 8 us per call is fixed (launch, ramp of the first wave's look-back), and the FP64 "
+                "carries cost about 3 % (float carries: 3 us less at 2^26): 2^28 below"}
     del dxf, dg, dyf, dgx, yf, ref
     n4 = 1 << 28
     hx4 = oracle.uniform_f32(n4, 2, -1.0, 1.0)
