@@ -17,13 +17,13 @@
 // Tile = R rows x 256 threads x V elements (V = 16 bytes / sizeof T), loaded
 // with coalesced 16-byte accesses: row r of the tile is one contiguous span of
 // 256*V elements, thread t holds elements [r*256*V + t*V, +V).  The staged
-// kernel's tiles of one vector are numbered by block index: blocks are
-// dispatched in index order, so a tile only waits on tiles whose blocks have
-// started, and the tile's copy is issued at once (an atomic ticket taken
-// first, as the register kernel and the segmented forms still do, put one L2
-// round trip in front of every tile's copy: 2^26 floats 102.4 against 98.2
-// us).  Were that order ever broken, the bounded waits below would end the
-// launch with SCL_DEV_ERR_TIMEOUT instead of a hang.
+// kernel's tiles are numbered by block index: blocks are dispatched in index
+// order, so a tile only waits on tiles whose blocks have started, and the
+// tile's copy is issued at once (an atomic ticket taken first, as the
+// register kernel still does, put one L2 round trip in front of every tile's
+// copy: 2^26 floats 102.4 against 98.2 us).  Were that order ever broken,
+// the bounded waits below would end the launch with SCL_DEV_ERR_TIMEOUT
+// instead of a hang.
 // In-tile: per-thread sequential fold, warp shuffles, one warp scans the R*8
 // warp totals, publishes the tile aggregate and looks back over up to 32
 // predecessors per round trip (one lane per predecessor).  Every wait is
@@ -187,8 +187,8 @@ __device__ __forceinline__ int scl_poll(const scl_scan_status& st, long long idx
   }
 }
 
-// Decoupled look-back of warp 0 (all 32 lanes) for the tile with ticket
-// `tile`, whose sequence starts at ticket `first`: returns the fold of every
+// Decoupled look-back of warp 0 (all 32 lanes) for tile number `tile`, whose
+// sequence starts at tile `first`: returns the fold of every
 // earlier tile of the sequence, combined as f(earlier, later).  Each round
 // reads 32 predecessors (one per lane, lane l = tile - 1 - l); a round that
 // finds an inclusive prefix ends the look-back, otherwise its aggregates are
@@ -607,9 +607,9 @@ scl_scan_short(const scl_T* in, scl_O* out, const scl_u64* seg_off, scl_u64 n_se
 // ordinary loads.  The host counts tiles with the same rule (scl_scan_tiles).
 //
 // SEG = 1: a segmented scan, one independent scan per segment
-// [seg_off[s], seg_off[s+1]) of the flat vector.  Segment s owns the tickets
+// [seg_off[s], seg_off[s+1]) of the flat vector.  Segment s owns the tiles
 // tile_start[s] .. tile_start[s+1]-1 (at least one), and the look-back stops
-// at the segment's first tile.  Tickets past the last tile (the grid is an
+// at the segment's first tile.  Blocks past the last tile (the grid is an
 // upper bound) return at once.
 // SEG = 2: the same (a segment plan numbered the tiles), and the blocks past
 // the tiles scan the segments of at most short_max elements, one window of
@@ -625,6 +625,7 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
   (void)aligned;
   (void)short_max;
   (void)win_rec;
+  (void)tile_counter;  // (the register kernel's ticket; the host passes both kernels the same arguments)
   constexpr int B = SCL_SCAN_B, W = SCL_SCAN_W;
   constexpr int V = scl_vec_width<sizeof(scl_T)>::value;
   constexpr int TILE = R * B * V;
@@ -642,15 +643,12 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
   __shared__ scl_T s_carry;  // the tile's prefix, converted once to the element type
   const unsigned int bar_s = (unsigned int)__cvta_generic_to_shared(&bar);
   if (threadIdx.x == 0) {
-    // one vector: the block index is the tile; segmented: the grid is an
-    // upper bound, blocks at or past the tile count take no ticket (all
-    // tickets below it go to the lower-numbered blocks, one each, in the
-    // order they start)
+    // the block index is the tile; segmented, the grid is an upper bound
+    // and blocks at or past the tile count take no tile
     if constexpr (SEG == 0) {
       s_tile = blockIdx.x;
     } else {
-      const bool take = blockIdx.x < tile_start[n_seg];
-      s_tile = take ? atomicAdd(tile_counter, 1u) : 0xffffffffu;
+      s_tile = blockIdx.x < tile_start[n_seg] ? blockIdx.x : 0xffffffffu;
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar_s));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -666,7 +664,7 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
   }
   __syncthreads();
   const unsigned int tile = s_tile;
-  unsigned int first = 0;  // ticket of the first tile of this tile's sequence
+  unsigned int first = 0;  // number of the first tile of this tile's sequence
   long long lo = 0, hi = (long long)n;  // the sequence's elements
   if constexpr (SEG != 0) {
     __shared__ long long s_seg;
