@@ -237,6 +237,7 @@ struct SegPlanCfg {
   int reverse = 0;
   unsigned int* tile_start = nullptr;  // device, n_seg + 1
   uint64_t tiles = 0;                  // tile_start[n_seg]
+  unsigned int* tile_seg = nullptr;    // device, `tiles` entries: each tile's segment
   // window records of the short segments (device, 4 words each: first
   // segment, end segment, first element, elements), one block each
   uint64_t n_rec = 0;

@@ -385,8 +385,9 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
     unsigned int* err = rt().dev_err;
     unsigned int spin = spin_of(tu);
     ArgPack pack;
+    void* towner = cfg->tile_seg;
     pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max, &wseg,
-                 &spin};
+                 &spin, &towner};
     if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
       return st;
     const uint64_t grid = cfg->tiles + cfg->n_rec;
@@ -444,8 +445,9 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
     ArgPack pack;
     void* no_windows = nullptr;
     unsigned int spin = spin_of(tu);
+    void* no_owners = nullptr;
     pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max,
-                 &no_windows, &spin};
+                 &no_windows, &spin, &no_owners};
     if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
       return st;
     p->last_variant = SCL_VARIANT_VECTOR;
@@ -686,6 +688,7 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   void* tile_start = prepass ? (char*)ws.ptr + total + seg_of : (plan ? (void*)pcfg->tile_start : nullptr);
   uint64_t short_max = plan ? pcfg->short_max : (n_seg ? kSegShort : 0);
   void* win_seg = plan ? (void*)pcfg->win_rec : nullptr;
+  void* tile_owner = plan ? (void*)pcfg->tile_seg : nullptr;
   uint64_t grid = tiles;
   if (plan) {
     // the blocks past the tiles take one window record of short segments
@@ -723,6 +726,7 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
     pack.ptrs.push_back(&n_seg);
     pack.ptrs.push_back(&short_max);
     pack.ptrs.push_back(&win_seg);
+    pack.ptrs.push_back(&tile_owner);
   }
   if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
     return st;

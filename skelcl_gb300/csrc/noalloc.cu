@@ -156,6 +156,7 @@ extern "C" int scl_launch_scan_noalloc(scl_program* p, const scl_shape* sh, void
     pack.ptrs.push_back(&n_seg);
     pack.ptrs.push_back(&short_max);
     pack.ptrs.push_back(&tile_start);  // (no window table)
+    pack.ptrs.push_back(&tile_start);  // (no tile owners)
   }
   if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
     return st;

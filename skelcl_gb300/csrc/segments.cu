@@ -251,6 +251,15 @@ broadcast_segments_kernel(const T* __restrict__ g, T* __restrict__ gx, const uin
   }
 }
 
+// tile_seg[t] = s for every tile t of segment s (tiles tile_start[s] ..
+// tile_start[s+1]-1), one thread per segment.
+__global__ void __launch_bounds__(256) seg_tile_owner_kernel(const unsigned int* __restrict__ tile_start,
+                                                             uint64_t n_seg, unsigned int* __restrict__ tile_seg) {
+  for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n_seg;
+       s += (uint64_t)gridDim.x * blockDim.x)
+    for (unsigned int t = tile_start[s]; t < tile_start[s + 1]; ++t) tile_seg[t] = (unsigned int)s;
+}
+
 }  // namespace
 
 size_t segments_prepare_scratch(uint64_t n_seg) {
@@ -291,6 +300,7 @@ void free_plan(SegPlan* p) {
   for (auto& c : p->cfgs) {
     cudaFree(c.tile_start);
     cudaFree(c.win_rec);
+    cudaFree(c.tile_seg);
   }
 }
 }  // namespace
@@ -373,6 +383,22 @@ int segplan_config(SegPlan* p, uint64_t tile, uint64_t vg, uint64_t a, int rever
                            rt().stream));
   SCL_CUDA(cudaStreamSynchronize(rt().stream));
   c.tiles = tiles;
+  // each tile's segment, so that a tile finds its segment with one load
+  if (tiles) {
+    rt().device_allocs++;
+    cudaError_t e = cudaMalloc(&c.tile_seg, (size_t)tiles * sizeof(unsigned int));
+    if (e == cudaSuccess) {
+      const uint64_t nb = std::min<uint64_t>((p->n_seg + 255) / 256, 65535);
+      seg_tile_owner_kernel<<<(unsigned)nb, 256, 0, rt().stream>>>(c.tile_start, p->n_seg, c.tile_seg);
+      e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+      cudaFree(c.tile_start);
+      cudaFree(c.win_rec);
+      cudaFree(c.tile_seg);
+      return cuda_fail(e, "segment plan: tile owners");
+    }
+  }
   p->cfgs.push_back(c);
   *out = &p->cfgs.back();
   return SCL_OK;

@@ -395,7 +395,8 @@ __global__ void __launch_bounds__(256)
 scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
                const unsigned int* tile_start, scl_u64 n_seg, int aligned, scl_C* partials,
                unsigned int* tickets, unsigned int* err, scl_u64 short_max,
-               const scl_u64* win_rec, unsigned int spin_limit SCL_EXTRA_PARAMS) {
+               const scl_u64* win_rec, unsigned int spin_limit,
+               const unsigned int* tile_seg SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
   (void)short_max;
   (void)win_rec;
@@ -417,12 +418,16 @@ scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
   if (threadIdx.x == 0) {
     long long sg = -1;
     if (tile < tile_start[n_seg]) {
-      scl_u64 lo = 0, hi = n_seg - 1;
-      while (lo < hi) {
-        const scl_u64 mid = (lo + hi + 1) / 2;
-        if (tile_start[mid] <= tile) lo = mid; else hi = mid - 1;
+      if (tile_seg) {  // (a segment plan's table)
+        sg = (long long)tile_seg[tile];
+      } else {
+        scl_u64 lo = 0, hi = n_seg - 1;
+        while (lo < hi) {
+          const scl_u64 mid = (lo + hi + 1) / 2;
+          if (tile_start[mid] <= tile) lo = mid; else hi = mid - 1;
+        }
+        sg = (long long)lo;
       }
-      sg = (long long)lo;
     }
     s_seg = sg;
   }

@@ -620,11 +620,13 @@ __global__ void __launch_bounds__(SCL_SCAN_B, MINB)
 scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int aligned,
            unsigned int* tile_counter, scl_scan_status st, scl_scan_clear clr, unsigned int spin_limit,
            unsigned int* err, const scl_u64* seg_off, const unsigned int* tile_start,
-           scl_u64 n_seg, scl_u64 short_max, const scl_u64* win_rec SCL_EXTRA_PARAMS) {
+           scl_u64 n_seg, scl_u64 short_max, const scl_u64* win_rec,
+           const unsigned int* tile_seg SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
   (void)aligned;
   (void)short_max;
   (void)win_rec;
+  (void)tile_seg;
   (void)tile_counter;  // (the register kernel's ticket; the host passes both kernels the same arguments)
   constexpr int B = SCL_SCAN_B, W = SCL_SCAN_W;
   constexpr int V = scl_vec_width<sizeof(scl_T)>::value;
@@ -671,12 +673,16 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
     if (threadIdx.x == 0) {
       long long sg = -1;
       if (tile < tile_start[n_seg]) {
-        scl_u64 l = 0, h = n_seg - 1;  // largest s with tile_start[s] <= tile
-        while (l < h) {
-          const scl_u64 mid = (l + h + 1) / 2;
-          if (tile_start[mid] <= tile) l = mid; else h = mid - 1;
+        if (tile_seg) {  // (a segment plan's table)
+          sg = (long long)tile_seg[tile];
+        } else {
+          scl_u64 l = 0, h = n_seg - 1;  // largest s with tile_start[s] <= tile
+          while (l < h) {
+            const scl_u64 mid = (l + h + 1) / 2;
+            if (tile_start[mid] <= tile) l = mid; else h = mid - 1;
+          }
+          sg = (long long)l;
         }
-        sg = (long long)l;
       }
       s_seg = sg;
     }
