@@ -322,12 +322,14 @@ int scl_launch_scan_noalloc(scl_program* prog, const scl_shape* shape,
  *      scl_sync) and returns a plan id.  A shape with seg_plan = that id (the
  *      same n_segments, and n at least the plan's) runs its segmented Scan or
  *      Reduce as ONE
- *      launch: the tiles of the long segments first, then a warp per segment
- *      of up to 4096 elements.  The plan keeps, per tile shape, which tiles
- *      belong to which segment; the first launch with a tile shape builds
- *      that (three small launches and a read-back of the tile count), so make
- *      it before capturing a graph.  Later changes to the caller's offsets
- *      are not seen: release the plan and create another. */
+ *      launch: the tiles of the long segments first, then one block per
+ *      window of segments of up to 4096 elements (a thread per segment of up
+ *      to 256 elements, a warp per longer one).  The plan keeps, per tile
+ *      shape, which tiles belong to which segment (and each tile's segment)
+ *      and the windows; the first launch with a tile shape builds them (four
+ *      small launches and a read-back of the offsets), so make it before
+ *      capturing a graph.  Later changes to the caller's offsets are not
+ *      seen: release the plan and create another. */
 int scl_segplan_create(const uint64_t* seg_offsets, uint64_t n_segments, uint64_t n,
                        uint32_t* plan);
 int scl_segplan_release(uint32_t plan);
