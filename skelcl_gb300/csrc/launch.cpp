@@ -386,8 +386,9 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
     unsigned int spin = spin_of(tu);
     ArgPack pack;
     void* towner = cfg->tile_seg;
+    unsigned int ntiles = (unsigned int)cfg->tiles;
     pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max, &wseg,
-                 &spin, &towner};
+                 &spin, &towner, &ntiles};
     if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
       return st;
     const uint64_t grid = cfg->tiles + cfg->n_rec;
@@ -446,8 +447,9 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
     void* no_windows = nullptr;
     unsigned int spin = spin_of(tu);
     void* no_owners = nullptr;
+    unsigned int ntiles = ~0u;  // (counted on the device by the pre-pass)
     pack.ptrs = {&in, &out, &offs, &tstart, &n_seg, &aligned, &partials, &tickets, &err, &short_max,
-                 &no_windows, &spin, &no_owners};
+                 &no_windows, &spin, &no_owners, &ntiles};
     if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
       return st;
     p->last_variant = SCL_VARIANT_VECTOR;
@@ -689,6 +691,7 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   uint64_t short_max = plan ? pcfg->short_max : (n_seg ? kSegShort : 0);
   void* win_seg = plan ? (void*)pcfg->win_rec : nullptr;
   void* tile_owner = plan ? (void*)pcfg->tile_seg : nullptr;
+  unsigned int n_tiles = plan ? (unsigned int)pcfg->tiles : ~0u;
   uint64_t grid = tiles;
   if (plan) {
     // the blocks past the tiles take one window record of short segments
@@ -727,6 +730,7 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
     pack.ptrs.push_back(&short_max);
     pack.ptrs.push_back(&win_seg);
     pack.ptrs.push_back(&tile_owner);
+    pack.ptrs.push_back(&n_tiles);
   }
   if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
     return st;

@@ -148,6 +148,7 @@ extern "C" int scl_launch_scan_noalloc(scl_program* p, const scl_shape* sh, void
   const void* seg_off = nullptr;
   const void* tile_start = nullptr;
   uint64_t n_seg = 0, short_max = 0;
+  unsigned int no_tiles = ~0u;  // (not segmented: unused)
   ArgPack pack;
   pack.ptrs = {&in, &out, &n, &fl, &aligned, &ticket, &sargs, &clr, &spin, &err};
   if (staged) {
@@ -157,6 +158,7 @@ extern "C" int scl_launch_scan_noalloc(scl_program* p, const scl_shape* sh, void
     pack.ptrs.push_back(&short_max);
     pack.ptrs.push_back(&tile_start);  // (no window table)
     pack.ptrs.push_back(&tile_start);  // (no tile owners)
+    pack.ptrs.push_back(&no_tiles);
   }
   if (int st = pack_extra(p, fn, pack.ptrs.size(), (const unsigned char*)extra, extra_bytes, &pack))
     return st;

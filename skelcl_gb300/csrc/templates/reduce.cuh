@@ -396,13 +396,14 @@ scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
                const unsigned int* tile_start, scl_u64 n_seg, int aligned, scl_C* partials,
                unsigned int* tickets, unsigned int* err, scl_u64 short_max,
                const scl_u64* win_rec, unsigned int spin_limit,
-               const unsigned int* tile_seg SCL_EXTRA_PARAMS) {
+               const unsigned int* tile_seg, unsigned int n_tiles SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
   (void)short_max;
   (void)win_rec;
   (void)spin_limit;
+  // the tile count, from the host when a plan knows it (~0u: read it)
+  const unsigned int nt = n_tiles != ~0u ? n_tiles : tile_start[n_seg];
   if constexpr (MERGED != 0) {
-    const unsigned int nt = tile_start[n_seg];
     if (blockIdx.x >= nt) {  // (block-uniform: the whole block takes the window role)
       constexpr int WT = 8 * 256 * scl_vec_width<sizeof(scl_T)>::value;  // 32 KB of elements
       scl_reduce_window_run<WT>(in, out, seg_off, win_rec, blockIdx.x - nt,
@@ -417,7 +418,7 @@ scl_reduce_seg(const scl_T* in, scl_T* out, const scl_u64* seg_off,
   __shared__ long long s_seg;
   if (threadIdx.x == 0) {
     long long sg = -1;
-    if (tile < tile_start[n_seg]) {
+    if (tile < nt) {
       if (tile_seg) {  // (a segment plan's table)
         sg = (long long)tile_seg[tile];
       } else {

@@ -621,13 +621,18 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
            unsigned int* tile_counter, scl_scan_status st, scl_scan_clear clr, unsigned int spin_limit,
            unsigned int* err, const scl_u64* seg_off, const unsigned int* tile_start,
            scl_u64 n_seg, scl_u64 short_max, const scl_u64* win_rec,
-           const unsigned int* tile_seg SCL_EXTRA_PARAMS) {
+           const unsigned int* tile_seg, unsigned int n_tiles SCL_EXTRA_PARAMS) {
   SCL_EXTRA_SETUP
   (void)aligned;
   (void)short_max;
   (void)win_rec;
   (void)tile_seg;
-  (void)tile_counter;  // (the register kernel's ticket; the host passes both kernels the same arguments)
+  (void)tile_counter;
+  // segmented: the tile count, from the host when a plan knows it (~0u:
+  // read it from tile_start[n_seg])
+  unsigned int nt = 0;
+  if constexpr (SEG != 0) nt = n_tiles != ~0u ? n_tiles : tile_start[n_seg];
+  (void)n_tiles;  // (the register kernel's ticket; the host passes both kernels the same arguments)
   constexpr int B = SCL_SCAN_B, W = SCL_SCAN_W;
   constexpr int V = scl_vec_width<sizeof(scl_T)>::value;
   constexpr int TILE = R * B * V;
@@ -650,14 +655,13 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
     if constexpr (SEG == 0) {
       s_tile = blockIdx.x;
     } else {
-      s_tile = blockIdx.x < tile_start[n_seg] ? blockIdx.x : 0xffffffffu;
+      s_tile = blockIdx.x < nt ? blockIdx.x : 0xffffffffu;
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar_s));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   scl_scan_clear_other(clr);
   if constexpr (SEG == 2) {
-    const unsigned int nt = tile_start[n_seg];
     if (blockIdx.x >= nt) {  // (block-uniform: the whole block takes the window role)
       scl_scan_window_run<TILE>(in, out, seg_off, win_rec, blockIdx.x - nt, flags, ts, bar_s, spin_limit,
                                 err SCL_EXTRA_ARGS);
@@ -672,7 +676,7 @@ scl_scan_s(const scl_T* in, scl_O* out, scl_u64 n, unsigned int flags, int align
     __shared__ long long s_seg;
     if (threadIdx.x == 0) {
       long long sg = -1;
-      if (tile < tile_start[n_seg]) {
+      if (tile < nt) {
         if (tile_seg) {  // (a segment plan's table)
           sg = (long long)tile_seg[tile];
         } else {
