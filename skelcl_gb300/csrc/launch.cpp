@@ -395,8 +395,8 @@ static int launch_reduce_impl(scl_program* p, const scl_shape* sh, void* const* 
     if (grid == 0) return SCL_OK;  // (every vector is either a tile's or in a record)
     if (grid > 0x7fffffffull) return fail(SCL_ERR_ARG, "segmented reduce: too many tiles");
     p->last_variant = SCL_VARIANT_VECTOR;
-    // (staged elements plus one skipped word in 32)
-    return launch(fn, dim3((unsigned)grid), dim3(256), (wt + wt / 32) * tsz, pack);
+    // (a record's elements keep their 16-byte phase: one vector more)
+    return launch(fn, dim3((unsigned)grid), dim3(256), wt * tsz + 16, pack);
   }
   if (sh->n_segments) {
     // one result per segment, one launch (plus the offsets pre-pass)
@@ -695,11 +695,12 @@ static int launch_scan_impl(scl_program* p, const scl_shape* sh, void* const* bu
   uint64_t grid = tiles;
   if (plan) {
     // the blocks past the tiles take one window record of short segments
-    // each; their staged index skips one word in 32
+    // each; a record keeps its 16-byte phase in shared memory, so it needs
+    // one vector more than a tile
     grid = tiles + pcfg->n_rec;
     if (grid == 0) return SCL_OK;  // (every vector is either a tile's or in a record)
     if (grid > 0x7fffffffull) return fail(SCL_ERR_ARG, "segmented scan: too many tiles");
-    smem += smem / 32;
+    smem += 16;
   }
   if (prepass) {
     uint64_t* scratch = reinterpret_cast<uint64_t*>((char*)p->ws.ptr + total + seg_of + seg_ts);
