@@ -357,10 +357,11 @@ __device__ __forceinline__ bool scl_mbar_wait(unsigned int bar_s, unsigned int s
   return true;
 }
 
-// Starts bringing src[0 .. len) (len <= MAXLEN) into shared memory so that
-// src[p] lands at ts[p + shift]; returns shift, the elements between src
-// and the 16-byte boundary below it, so that 16-byte-aligned global addresses
-// meet 16-byte-aligned shared ones.  The 16-byte-aligned interior of the
+// Starts bringing src[0 .. len) into shared memory so that src[p] lands at
+// ts[p + shift] (ts 16-byte aligned, room for len + 16 / sizeof(T)
+// elements); returns shift, the elements between src and the 16-byte
+// boundary below it, so that 16-byte-aligned global addresses meet
+// 16-byte-aligned shared ones.  The 16-byte-aligned interior of the
 // range goes by bulk asynchronous copies that thread 0 issues on the
 // mbarrier bar_s (initialised by the caller, phase 0); *tx receives the bytes
 // it counts (0: nothing issued, no wait needed).  The ragged ends (under 16
@@ -368,7 +369,7 @@ __device__ __forceinline__ bool scl_mbar_wait(unsigned int bar_s, unsigned int s
 // outside the range is read.  Elements that do not tile 16 bytes, or do not
 // sit on their own size, are all read by ordinary loads (shift 0).  The
 // caller waits on the mbarrier (thread 0) and then synchronises the block.
-template <typename T, int MAXLEN, int B>
+template <typename T, int B>
 __device__ __forceinline__ int scl_stage_bulk(const T* src, int len, T* ts, unsigned int bar_s,
                                               unsigned int* tx) {
   constexpr int V = scl_vec_width<sizeof(T)>::value;
@@ -406,6 +407,7 @@ __device__ __forceinline__ int scl_stage_bulk(const T* src, int len, T* ts, unsi
   if ((int)threadIdx.x < ntail) ts[hi + threadIdx.x + shift] = src[hi + threadIdx.x];
   return shift;
 }
+
 __device__ __forceinline__ unsigned int scl_ld_acquire(const unsigned int* p) {
   unsigned int v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");

@@ -297,7 +297,7 @@ __device__ __forceinline__ void scl_reduce_window_run(const scl_T* in, scl_T* ou
   const scl_u64 ln = win_rec[4 * r + 3];
   const int len = (int)(ln < (scl_u64)WT ? ln : (scl_u64)WT);  // (more only for bad offsets)
   unsigned int tx;
-  const int shift = scl_stage_bulk<scl_T, WT, B>(in + e0, len, ts, bar_s, &tx);
+  const int shift = scl_stage_bulk<scl_T, B>(in + e0, len, ts, bar_s, &tx);
   // this thread's first vector's offsets are read while the copy lands
   scl_u64 sg = lo + threadIdx.x;
   scl_u64 a_n = 0, b_n = 0;

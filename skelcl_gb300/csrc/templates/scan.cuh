@@ -495,7 +495,7 @@ __device__ __forceinline__ void scl_scan_window_run(const scl_T* in, scl_O* out,
   if (len == 0) return;  // (block-uniform) nothing to write for empty vectors
   __shared__ int s_ok;
   unsigned int tx;
-  const int shift = scl_stage_bulk<scl_T, TILE, B>(in + e0, len, ts, bar_s, &tx);
+  const int shift = scl_stage_bulk<scl_T, B>(in + e0, len, ts, bar_s, &tx);
   // this thread's first vector's offsets are read while the copy lands
   scl_u64 sg = lo + threadIdx.x;
   scl_u64 a_n = 0, b_n = 0;
