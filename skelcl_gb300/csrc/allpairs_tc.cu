@@ -156,18 +156,40 @@ __global__ void __launch_bounds__(256) split_rows_kernel(const float* __restrict
 }
 
 // B (K x N row-major) -> parts of B^T ([part][Np][Kp]) through 64 x 64 tiles
-// in shared memory: coalesced row reads of B, 16-byte stores of 8
-// consecutive k per part.  Np and Kp are multiples of 64.
+// in shared memory: coalesced row reads of B (16 bytes at a time when rows
+// allow it), 16-byte stores of 8 consecutive k per part.  Np and Kp are
+// multiples of 64.
 __global__ void __launch_bounds__(256) split_transpose_kernel(const float* __restrict__ B, uint32_t K,
                                                               uint32_t N, uint32_t Np, uint32_t Kp,
                                                               int parts, __nv_bfloat16* __restrict__ out) {
   __shared__ float tile[64][65];  // [k][n]
   const uint32_t k0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
   const uint64_t plane = (uint64_t)Np * Kp;
-  for (int i = threadIdx.x; i < 64 * 64; i += 256) {
-    const uint32_t kk = (uint32_t)i / 64, nn = (uint32_t)i % 64;
-    const uint32_t k = k0 + kk, n = n0 + nn;
-    tile[kk][nn] = (k < K && n < N) ? B[(uint64_t)k * N + n] : 0.0f;
+  if ((N % 4u) == 0 && (reinterpret_cast<uintptr_t>(B) & 15u) == 0) {
+    // 16-byte loads, four rows per thread in flight (a full row of 64 is 16
+    // loads; n0 and N are multiples of 4, so a load is wholly in or out)
+    const uint32_t c4 = threadIdx.x % 16, r0 = threadIdx.x / 16;
+    float4 q[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const uint32_t k = k0 + r0 + 16 * i, n = n0 + c4 * 4;
+      q[i] = (k < K && n < N) ? *reinterpret_cast<const float4*>(B + (uint64_t)k * N + n)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      float* t = &tile[r0 + 16 * i][c4 * 4];
+      t[0] = q[i].x;
+      t[1] = q[i].y;
+      t[2] = q[i].z;
+      t[3] = q[i].w;
+    }
+  } else {
+    for (int i = threadIdx.x; i < 64 * 64; i += 256) {
+      const uint32_t kk = (uint32_t)i / 64, nn = (uint32_t)i % 64;
+      const uint32_t k = k0 + kk, n = n0 + nn;
+      tile[kk][nn] = (k < K && n < N) ? B[(uint64_t)k * N + n] : 0.0f;
+    }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < 64 * 8; i += 256) {
