@@ -333,6 +333,14 @@ int scl_launch_scan_noalloc(scl_program* prog, const scl_shape* shape,
 int scl_segplan_create(const uint64_t* seg_offsets, uint64_t n_segments, uint64_t n,
                        uint32_t* plan);
 int scl_segplan_release(uint32_t plan);
+/* The window records a segment plan makes of its short segments (host only,
+ * no device): for HOST offsets (n_segments + 1, clamped, non-decreasing)
+ * and short_max > 0 (a plan uses half a scan tile), *count receives the
+ * number of records and, when `records` is not NULL, up to `capacity`
+ * records of four words {first segment, end segment, first element,
+ * elements}.  For tests of the plan's host logic. */
+int scl_debug_window_records(const uint64_t* offsets, uint64_t n_segments, uint64_t short_max,
+                             uint64_t* records, uint64_t capacity, uint64_t* count);
 
 /* ---- adjoint building blocks (no counterpart in the reference; used by the
  *      reverse-mode tape in include/SkelCL/Adjoint.h).  Element types:   */

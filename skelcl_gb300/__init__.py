@@ -104,6 +104,7 @@ SIGNATURES = {
     "scl_launch_allpairs": ([_VP, ctypes.POINTER(Shape), ctypes.POINTER(_VP), _VP, _SZ, ctypes.POINTER(Tuning)], _I),
     "scl_launch_count": ([ctypes.POINTER(_U64)], _I),
     "scl_pdl_set": ([ctypes.c_int, ctypes.POINTER(ctypes.c_int)], _I),
+    "scl_debug_window_records": ([_VP, _U64, _U64, _VP, _U64, ctypes.POINTER(_U64)], _I),
     "scl_pdl_launch_count": ([ctypes.POINTER(_U64)], _I),
     "scl_debug_counters": ([ctypes.POINTER(_U64), ctypes.POINTER(_U64)], _I),
     "scl_debug_fp32_peak": ([_I, _U32, _VP, _U64, ctypes.POINTER(_U64)], _I),
@@ -174,6 +175,21 @@ def overlapped_launch_count() -> int:
     v = ctypes.c_uint64(0)
     check(lib().scl_pdl_launch_count(ctypes.byref(v)))
     return v.value
+
+
+def window_records(offsets, short_max: int):
+    """The window records a segment plan makes of its short segments, as an
+    (n, 4) uint64 array {first segment, end segment, first element,
+    elements}; host only."""
+    import numpy as np
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    n_seg = len(off) - 1
+    cnt = ctypes.c_uint64(0)
+    check(lib().scl_debug_window_records(off.ctypes.data, n_seg, short_max, None, 0, ctypes.byref(cnt)))
+    rec = np.zeros((cnt.value, 4), np.uint64)
+    check(lib().scl_debug_window_records(off.ctypes.data, n_seg, short_max, rec.ctypes.data, cnt.value,
+                                         ctypes.byref(cnt)))
+    return rec
 
 
 def sha1_hex(data: bytes) -> str:

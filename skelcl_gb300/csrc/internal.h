@@ -251,6 +251,11 @@ struct SegPlan {
   uint64_t* scratch = nullptr;
   std::deque<SegPlanCfg> cfgs;  // (stable addresses)
 };
+// The window records a segment plan makes of its short segments (four words
+// each: first segment, end segment, first element, elements).
+void segplan_window_records(const uint64_t* off, uint64_t n_seg, uint64_t short_max,
+                            std::vector<uint64_t>* rec);
+
 SegPlan* segplan_find(uint32_t id);
 // The plan's tile numbering for one tile shape, built on first use (three
 // small launches and a read-back of the tile count; refused inside a stream

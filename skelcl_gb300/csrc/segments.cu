@@ -305,6 +305,33 @@ void free_plan(SegPlan* p) {
 }
 }  // namespace
 
+// Window records of the short segments: consecutive segments starting in the
+// same window of short_max elements form one record {first segment, end
+// segment, first element, elements}; a last segment longer than short_max
+// belongs to the tiles and is left out (its start ends the record's
+// elements).  All but the last segment of a record end inside its window, so
+// a record spans at most 2 * short_max elements.  Records whose segments are
+// all empty stay (the Reduce writes their identities); windows that own no
+// segment get none.  `off` holds n_seg + 1 clamped offsets.
+void segplan_window_records(const uint64_t* off, uint64_t n_seg, uint64_t short_max,
+                            std::vector<uint64_t>* rec) {
+  rec->clear();
+  for (uint64_t sg = 0; sg < n_seg;) {
+    const uint64_t w = off[sg] / short_max, w0 = w * short_max, w1 = w0 + short_max;
+    uint64_t hi = sg + 1;
+    while (hi < n_seg && off[hi] >= w0 && off[hi] < w1) ++hi;
+    const uint64_t la = off[hi - 1], lb = std::max(la, off[hi]);
+    const uint64_t top = lb - la > short_max ? hi - 1 : hi;
+    if (top > sg) {
+      const uint64_t e0 = off[sg];
+      uint64_t e1 = top == hi ? lb : off[top];
+      if (e1 < e0) e1 = e0;
+      rec->insert(rec->end(), {sg, top, e0, e1 - e0});
+    }
+    sg = hi;
+  }
+}
+
 SegPlan* segplan_find(uint32_t id) {
   std::lock_guard<std::mutex> g(g_plan_mu);
   auto it = g_plans.find(id);
@@ -337,33 +364,13 @@ int segplan_config(SegPlan* p, uint64_t tile, uint64_t vg, uint64_t a, int rever
     cudaFree(c.tile_start);
     return st;
   }
-  // Window records of the short segments (on the host, once): consecutive
-  // segments starting in the same window of short_max elements form one
-  // record {first segment, end segment, first element, elements}; a last
-  // segment longer than short_max belongs to the tiles and is left out (its
-  // start ends the record's elements).  All but the last segment of a record
-  // end inside its window, so a record spans at most 2 * short_max elements.
-  // Records whose segments are all empty stay (the Reduce writes their
-  // identities); windows that own no segment get none.
+  // the window records of the short segments (on the host, once)
   std::vector<uint64_t> off(p->n_seg + 1);
   SCL_CUDA(cudaMemcpyAsync(off.data(), p->off, off.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost,
                            rt().stream));
   SCL_CUDA(cudaStreamSynchronize(rt().stream));
   std::vector<uint64_t> rec;
-  for (uint64_t sg = 0; sg < p->n_seg;) {
-    const uint64_t w = off[sg] / short_max, w0 = w * short_max, w1 = w0 + short_max;
-    uint64_t hi = sg + 1;
-    while (hi < p->n_seg && off[hi] >= w0 && off[hi] < w1) ++hi;
-    const uint64_t la = off[hi - 1], lb = std::max(la, off[hi]);
-    const uint64_t top = lb - la > short_max ? hi - 1 : hi;
-    if (top > sg) {
-      const uint64_t e0 = off[sg];
-      uint64_t e1 = top == hi ? lb : off[top];
-      if (e1 < e0) e1 = e0;
-      rec.insert(rec.end(), {sg, top, e0, e1 - e0});
-    }
-    sg = hi;
-  }
+  segplan_window_records(off.data(), p->n_seg, short_max, &rec);
   c.n_rec = rec.size() / 4;
   if (c.n_rec) {
     rt().device_allocs++;
@@ -479,5 +486,19 @@ extern "C" int scl_adjoint_broadcast_segments(const void* g, void* gx, const uin
         (const double*)g, (double*)gx, seg_offsets, n_segments, n, acc, aligned);
   SCL_CUDA(cudaGetLastError());
   ++rt().launches;
+  return SCL_OK;
+}
+
+extern "C" int scl_debug_window_records(const uint64_t* offsets, uint64_t n_segments, uint64_t short_max,
+                                        uint64_t* records, uint64_t capacity, uint64_t* count) {
+  if (!offsets || !count) return fail(SCL_ERR_ARG, "scl_debug_window_records: null argument");
+  if (short_max == 0) return fail(SCL_ERR_ARG, "scl_debug_window_records: short_max must be positive");
+  std::vector<uint64_t> rec;
+  segplan_window_records(offsets, n_segments, short_max, &rec);
+  *count = rec.size() / 4;
+  if (records) {
+    if (capacity < *count) return fail(SCL_ERR_ARG, "scl_debug_window_records: capacity too small");
+    std::memcpy(records, rec.data(), rec.size() * sizeof(uint64_t));
+  }
   return SCL_OK;
 }
